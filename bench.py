@@ -1,0 +1,355 @@
+"""Benchmark of the GB300 NTT library (one JSON line on stdout).
+
+Workload (one step): the batched radix-4 int16 forward NTT of 4096 polynomials
+x 4 RNS moduli {7681, 10753, 12289, 12289}.  7681 and 10753 have no 1024-th
+root of unity (their largest power-of-two root order is 512) and radix-4 needs
+n = 4^k, so their lanes run at n = 256; the two 12289 lanes run at n = 1024.
+Inputs are seeded uniform residues, resident in HBM; L2 is flushed (256 MiB
+write) before every timed step.  A step is the whole batch (16384 NTTs).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's algorithm on the host cores: the
+reference's own kernels need AMD's AIE toolchain, so its CPU restatement in
+oracle/ (the parity oracle) is run with all host threads instead.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+SEGMENTS = [  # (q, n, polynomials, generator of Z_q^*)
+    (7681, 256, 4096, 17),
+    (10753, 256, 4096, 11),
+    (12289, 1024, 8192, 41),
+]
+SEED = 20261203
+METRIC = "batched NTT/s & HBM GB/s vs plain per-NTT launch (bit-exact); p50/p99 serve latency"
+WORKLOAD = ("batched radix-4 int16 forward NTT: 4096 polys x 4 moduli {7681,10753,12289,12289}; "
+            "n=256 for 7681/10753 (no 1024-th root of unity), n=1024 for 12289")
+
+
+def root_of(q, n, g):
+    if q == 12289:
+        return pow(41, 4096 // n, q)
+    return pow(g, (q - 1) // n, q)
+
+
+def make_inputs():
+    rng = np.random.default_rng(SEED)
+    return [rng.integers(0, q, size=(cnt, n)).astype(np.int16) for q, n, cnt, _ in SEGMENTS]
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic():
+    try:
+        with open(os.path.join(HERE, "profiles", "traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms in the background."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.samples = []
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append((time.time(), parts))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        inside = [s for t, s in self.samples if t0 <= t <= t1]
+        note = "sampled during the timed region"
+        if not inside:
+            inside = [s for t, s in self.samples if t1 - 2.0 <= t <= t1 + 0.2]
+            note = "timed region shorter than the sampling period: samples from the surrounding load"
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "note": "nvidia-smi unavailable"}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(s[1]) for s in inside if num(s[1]) is not None]
+        mx = [num(s[2]) for s in inside if num(s[2]) is not None]
+        reasons = sorted({names[i] for s in inside for i in range(4) if s[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(inside), "note": note}
+
+
+def cpu_baseline(inputs, seconds, threads):
+    """The oracle (CPU restatement of the reference's loops) over all host threads,
+    whole batches until `seconds` have passed."""
+    from oracle import oracle
+    plans = [oracle.Plan(oracle.R4_I16_FWD, n, q, root_of(q, n, g)) for (q, n, _, g) in SEGMENTS]
+    done, t0 = 0, time.perf_counter()
+    while True:
+        for p, x in zip(plans, inputs):
+            p(x, threads=threads)
+        done += sum(x.shape[0] for x in inputs)
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            return done / el, done, el
+
+
+def run_reference(args):
+    """--impl reference: the reference's algorithm (oracle restatement) on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    inputs = make_inputs()
+    from oracle import oracle
+    plans = [oracle.Plan(oracle.R4_I16_FWD, n, q, root_of(q, n, g)) for (q, n, _, g) in SEGMENTS]
+    # size each step so that warmup + steps stay within about two minutes
+    t0 = time.perf_counter()
+    for p, x in zip(plans, inputs):
+        p(x, threads=threads)
+    full = time.perf_counter() - t0
+    budget = 120.0
+    frac = 1.0
+    if full * (args.steps + args.warmup) > budget:
+        frac = max(1e-3, budget / (full * (args.steps + args.warmup)))
+    sample = [x[: max(1, int(x.shape[0] * frac))] for x in inputs]
+    per_step = sum(s.shape[0] for s in sample)
+    for _ in range(args.warmup):
+        for p, x in zip(plans, sample):
+            p(x, threads=threads)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        for p, x in zip(plans, sample):
+            p(x, threads=threads)
+        times.append(time.perf_counter() - t)
+    ms = 1e3 * sum(times) / len(times)
+    value = per_step / (ms / 1e3)
+    desc = f"{per_step} of the 16384 NTTs per step ({frac:.3f} of every segment)"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "NTT/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int16", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "polys_per_step": per_step},
+        "cpu_baseline": {"value": value, "unit": "NTT/s", "cores": threads, "kind": "port",
+                         "sample": desc + "; the reference's AIE kernels cannot be built here, so its CPU "
+                                          "restatement (oracle/ntt_oracle.c, the parity oracle) is timed"},
+        "e2e": {"value": value, "unit": "NTT/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    import ntts_on_amd_ai_engines_aie1_gb300 as gb
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    inputs = make_inputs()
+    plans = [gb.Plan(gb.Kind.R4_I16_FWD, n, q, root_of(q, n, g)) for (q, n, _, g) in SEGMENTS]
+    d_in = [torch.from_numpy(x).to(dev) for x in inputs]
+    d_out = [torch.empty_like(x) for x in d_in]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    polys = sum(cnt for _, _, cnt, _ in SEGMENTS)
+    algo_bytes = sum(2 * n * 2 * cnt for _, n, cnt, _ in SEGMENTS)
+    dom = 2  # dominant kernel: the n = 1024, q = 12289 segment
+    dom_bytes = 2 * SEGMENTS[dom][1] * 2 * SEGMENTS[dom][2]
+
+    # correctness gate on the timed data (bit-exact vs the oracle on a sample)
+    from oracle import oracle
+    for i, (q, n, _, g) in enumerate(SEGMENTS):
+        plans[i](d_in[i], out=d_out[i])
+    torch.cuda.synchronize()
+    for i, (q, n, _, g) in enumerate(SEGMENTS):
+        want = oracle.Plan(oracle.R4_I16_FWD, n, q, root_of(q, n, g))(inputs[i][:64])
+        assert np.array_equal(d_out[i][:64].cpu().numpy(), want), "GPU output differs from the oracle"
+
+    def step():
+        for i in range(len(SEGMENTS)):
+            plans[i].execute(d_in[i], d_out[i], SEGMENTS[i][2], stream)
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    time.sleep(0.3)
+    # keep the GPU loaded briefly so the sampler sees clocks under load
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = gb.launch_count()
+    t_wall0 = time.time()
+    for i in range(args.steps):
+        flush.zero_()
+        e0, e1, k0, k1 = ev[i]
+        e0.record(stream)
+        plans[0].execute(d_in[0], d_out[0], SEGMENTS[0][2], stream)
+        plans[1].execute(d_in[1], d_out[1], SEGMENTS[1][2], stream)
+        k0.record(stream)
+        plans[2].execute(d_in[2], d_out[2], SEGMENTS[2][2], stream)
+        k1.record(stream)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    t_wall1 = time.time()
+    launches = gb.launch_count() - launches0
+    if dist:
+        dist.barrier()
+    sampler.stop()
+    step_ms = [a.elapsed_time(b) for a, b, _, _ in ev]
+    dom_ms = [c.elapsed_time(d) for _, _, c, d in ev]
+    ms = sum(step_ms) / len(step_ms)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * polys / (ms / 1e3)
+    dom_avg = sum(dom_ms) / len(dom_ms)
+    peak, peak_src = load_peaks()
+    achieved = dom_bytes / (dom_avg / 1e3) / 1e9
+    traffic = load_traffic()
+
+    # plain per-NTT launches of the same batch (the baseline the metric names)
+    per_ntt = None
+    if rank == 0 and not args.skip_per_ntt:
+        flush.zero_()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for i, (q, n, cnt, _) in enumerate(SEGMENTS):
+            bs = n * 2
+            base_in, base_out = d_in[i].data_ptr(), d_out[i].data_ptr()
+            for j in range(cnt):
+                plans[i].execute(base_in + j * bs, base_out + j * bs, 1, stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        pm = a.elapsed_time(b)
+        per_ntt = {"value": polys / (pm / 1e3), "unit": "NTT/s", "launches": polys,
+                   "batched_speedup": (polys / (ms / 1e3)) / (polys / (pm / 1e3))}
+
+    # end to end through the C ABI on pinned host buffers
+    h_in = [torch.from_numpy(x).pin_memory() for x in inputs]
+    h_out = [torch.empty_like(x).pin_memory() for x in h_in]
+    e2e_steps = max(3, min(args.steps, 100))
+    for _ in range(min(args.warmup, 5)):
+        for i in range(len(SEGMENTS)):
+            plans[i].execute_host(h_in[i], h_out[i], SEGMENTS[i][2], stream)
+    e2e_t = []
+    for _ in range(e2e_steps):
+        t0 = time.perf_counter()
+        for i in range(len(SEGMENTS)):
+            plans[i].execute_host(h_in[i], h_out[i], SEGMENTS[i][2], stream)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * sum(e2e_t) / len(e2e_t)
+    assert np.array_equal(h_out[2][:64].numpy(), oracle.Plan(oracle.R4_I16_FWD, 1024, 12289, 11580)(inputs[2][:64]))
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    threads = os.cpu_count() or 1
+    cpu = None
+    if not args.skip_cpu:
+        v, done, el = cpu_baseline(inputs, args.cpu_seconds, threads)
+        cpu = {"value": v, "unit": "NTT/s", "cores": threads, "kind": "port",
+               "sample": f"{done} NTTs of the same workload in {el:.1f} s (whole batches), oracle/ntt_oracle.c "
+                         f"with {threads} threads; the reference's AIE kernels cannot be built here"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "NTT/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int16", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "polys_per_step": polys, "coefficients_per_step": polys and
+                   sum(n * cnt for _, n, cnt, _ in SEGMENTS), "algorithmic_bytes_per_step": algo_bytes,
+                   "hbm_gbs_whole_step": algo_bytes / (ms / 1e3) / 1e9,
+                   "l2": "flushed before every step (256 MiB write, untimed)", "parallelism": f"replicas{world}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_src,
+                     "kernel": "k_ntt radix-4 n=1024 q=12289 (8192 polys per launch)",
+                     "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": dom_avg,
+                     "traffic": (traffic or {}).get("bytes_per_launch")},
+        "cpu_baseline": cpu,
+        "e2e": {"value": polys / (e2e_ms / 1e3), "unit": "NTT/s", "h2d_bytes_per_step": algo_bytes // 2,
+                "d2h_bytes_per_step": algo_bytes // 2, "ms_per_step": e2e_ms, "steps": e2e_steps,
+                "api": "gbntt_execute_host per segment (pinned host buffers)"},
+        "per_ntt_launch": per_ntt,
+        "gpu_launches": launches,
+        "clocks": sampler.summary(t_wall0, t_wall1),
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-seconds", type=float, default=6.0)
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-per-ntt", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

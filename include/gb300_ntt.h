@@ -1,0 +1,135 @@
+/*
+ * gb300_ntt.h -- C ABI of the GB300 NTT library (libgb300ntt.so).
+ *
+ * The library re-implements, for one NVIDIA GB300 (sm_103a), the designs of
+ * the AIE1 NTT artifact: radix-2 int16/int32 forward and inverse pipelines,
+ * radix-4 and radix-8 int16 forward pipelines, and the stand-alone
+ * bit-reversal and full-Barrett units.  Each design of the reference is an
+ * ADF graph class whose constructor computes the twiddle/Barrett tables, whose
+ * ports carry one polynomial per graph iteration, and whose lifecycle is
+ * graph.init(); graph.run(N); graph.end() (src/project.cpp:161-164).  Here:
+ *
+ *   graph constructor + init()   ->  gbntt_plan_create()   (tables built once,
+ *                                    kept resident in device memory)
+ *   graph.run(N) over in_data /  ->  gbntt_execute()        (N polynomials per
+ *   out_data ports                   call, one fused kernel launch)
+ *   graph.end()                  ->  gbntt_plan_destroy()
+ *
+ * Conventions.  Polynomials are contiguous arrays of int16_t (int16 designs)
+ * or int32_t (int32 designs); a batch is `batch` polynomials back to back.
+ * Forward transforms take natural-order input and return bit-reversed output;
+ * inverse transforms take bit-reversed input, return natural order, and omit
+ * the factor n^-1 (reference README.md:157-160).  By default outputs are the
+ * reference's partially reduced values, bit for bit; GBNTT_FLAG_CANONICAL
+ * returns the same residues reduced to [0, q).  d_in is read-only; d_in ==
+ * d_out (in place) is allowed.  Plans are immutable after creation and may be
+ * used from several host threads and streams at once.  Every function returns
+ * a gbntt_status; gbntt_last_error() gives a message for the calling thread.
+ */
+#ifndef GB300_NTT_H
+#define GB300_NTT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBNTT_ABI_VERSION 1
+
+/* Design kinds.  0..7 are the reference's NTT_CONFIG values
+ * (src/project.cpp:35, :139-157; README.md:117-126). */
+typedef enum gbntt_kind {
+    GBNTT_R2_I16_FWD = 0,       /* NTT<n,q,w,...,TYPE_NTT_NO_to_BO>        src/ntt.h:43            */
+    GBNTT_R2_I16_INV = 1,       /* NTT<n,q,w,...,TYPE_INTT_BO_to_NO>       src/ntt.h:43            */
+    GBNTT_R4_I16_FWD = 2,       /* NTT_R4<n,q,w,...,FORWARD_CT_NO_TO_BO>   src/ntt_r4.h:30         */
+    GBNTT_R8_I16_STAGE = 3,     /* NTT_R8<q,n,w>: one radix-8 stage        src/ntt_r8.h:22         */
+    GBNTT_R2_I32_FWD = 4,       /* NTT_INT32<...,FORWARD_CT_NO_TO_BO>      src/ntt_int32.h:27      */
+    GBNTT_R2_I32_INV = 5,       /* NTT_INT32<...,INVERSE_GS_BO_TO_NO>      src/ntt_int32.h:27      */
+    GBNTT_BITREV_I16 = 6,       /* BITREVERSE<n>                           src/standalone_units.h:17 */
+    GBNTT_FULL_BARRETT_I16 = 7, /* FULL_BARRETT_MULTIPLICATION<n,q,F>      src/standalone_units.h:40 */
+    /* Designs the reference describes but does not ship as a graph: */
+    GBNTT_R8_I16_FWD = 8,       /* all radix-8 stages chained, plus a radix-2/4 tail stage when
+                                   log2 n is not a multiple of 3 (src/ntt_r8.h:15-19)           */
+    GBNTT_R4_I16_INV = 9        /* bit-reversal + radix-4 forward with inverse twiddles, then
+                                   bit-reversal to natural order (src/ntt_r4.h:18-20)           */
+} gbntt_kind;
+
+typedef enum gbntt_status {
+    GBNTT_OK = 0,
+    GBNTT_ERR_ARG = 1,        /* null pointer or argument out of range                         */
+    GBNTT_ERR_LENGTH = 2,     /* n not a power of two or not supported by the design
+                                 (src/auxiliary.h:11, src/kernels/bitreverse_kernels.cc:58)    */
+    GBNTT_ERR_MODULUS = 3,    /* q not an odd prime candidate or above the lazy-reduction bound
+                                 of the storage type (src/ntt.h:118, src/ntt_int32.h:16)       */
+    GBNTT_ERR_ROOT = 4,       /* root is not of order exactly n ("ROOT is not correct",
+                                 src/auxiliary.h:37,44)                                         */
+    GBNTT_ERR_LAYERS = 5,     /* radix-4 needs an even number of radix-2 layers
+                                 (src/ntt_r4.h:62-63)                                           */
+    GBNTT_ERR_KIND = 6,       /* unknown design kind                                            */
+    GBNTT_ERR_CUDA = 7,       /* CUDA runtime error (message in gbntt_last_error)               */
+    GBNTT_ERR_NOMEM = 8,      /* device or host allocation failed                              */
+    GBNTT_ERR_TIMEOUT = 9,    /* a bounded wait ran out                                         */
+    GBNTT_ERR_ADMISSION = 10  /* a request could not be admitted (not enough free memory)       */
+} gbntt_status;
+
+/* Plan flags */
+#define GBNTT_FLAG_CANONICAL   0x1u  /* reduce outputs to [0, q)                                   */
+#define GBNTT_FLAG_R8_EXACT    0x2u  /* exact K=31 radix-8 multipliers (default for R8_I16_FWD)    */
+#define GBNTT_FLAG_R8_FLOAT    0x4u  /* the reference's float K=31 multipliers (src/twiddle.h:372;
+                                        default for R8_I16_STAGE)                                  */
+
+typedef struct gbntt_plan gbntt_plan;
+
+/* Builds a plan: validates (kind, n, q, root), computes the reference's
+ * tables on the host, uploads them to the current device (they stay resident
+ * until gbntt_plan_destroy).  `root` is a primitive n-th root of unity modulo
+ * q (the inverse designs invert it themselves, like src/twiddle.h:80,112).
+ * `factor` is the multiplier of GBNTT_FULL_BARRETT_I16 (e.g. n^-1 mod q,
+ * src/project.cpp:154); ignored otherwise.  BITREV_I16 ignores q and root. */
+int gbntt_plan_create(gbntt_plan** plan, int kind, uint32_t n, int64_t q, int64_t root,
+                      int64_t factor, uint32_t flags);
+
+/* Releases the plan's device tables.  NULL is accepted. */
+int gbntt_plan_destroy(gbntt_plan* plan);
+
+/* Transforms `batch` polynomials held in device memory, asynchronously on
+ * `stream` (a cudaStream_t; NULL = legacy default stream).  One kernel launch
+ * per call (two for R2_I32 with n > 8192). */
+int gbntt_execute(const gbntt_plan* plan, const void* d_in, void* d_out, uint64_t batch,
+                  void* stream);
+
+/* Same, on host buffers: copies the inputs to device staging memory owned by
+ * the plan, transforms, copies back and waits for the stream.  Pinned host
+ * buffers give full copy bandwidth.  Serialised per plan. */
+int gbntt_execute_host(gbntt_plan* plan, const void* h_in, void* h_out, uint64_t batch,
+                       void* stream);
+
+/* Plan properties. */
+#define GBNTT_Q_N           0  /* n                                    */
+#define GBNTT_Q_MODULUS     1  /* q                                    */
+#define GBNTT_Q_ELEM_BYTES  2  /* 2 (int16 designs) or 4 (int32)       */
+#define GBNTT_Q_STAGES      3  /* pipeline stages of the reference design (tiles) */
+#define GBNTT_Q_KIND        4
+#define GBNTT_Q_TABLE_BYTES 5  /* device bytes held by the plan's tables */
+int gbntt_plan_query(const gbntt_plan* plan, int what, int64_t* value);
+
+/* Host-side tables, without any CUDA call (for checking the table code on a
+ * machine without a GPU).  which = 0: the device twiddle table as (tw, w')
+ * pairs flattened; 1: the scalar constants.  Writes at most cap values and
+ * stores the full length in *len. */
+int gbntt_host_tables(int kind, uint32_t n, int64_t q, int64_t root, int64_t factor,
+                      uint32_t flags, int which, int64_t* dst, int64_t cap, int64_t* len);
+
+/* Total number of kernels this library has launched in this process. */
+uint64_t gbntt_launch_count(void);
+
+const char* gbntt_last_error(void);
+const char* gbntt_status_string(int status);
+int gbntt_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GB300_NTT_H */

@@ -1,0 +1,309 @@
+"""GB300 NTT library: Python host side over the C ABI of libgb300ntt.so.
+
+The reference builds one ADF graph per design, constructed with compile-time
+template parameters and run with ``graph.init(); graph.run(N); graph.end()``
+(src/project.cpp:161-164).  This module mirrors those graph classes:
+
+    NTT(LENGTH, MODULUS, ROOT, NTT_TYPE.TYPE_NTT_NO_to_BO)          src/ntt.h:43
+    NTT_INT32(LENGTH, MODULUS, ROOT, NTT_INT32_TYPE.FORWARD_CT_NO_TO_BO)   src/ntt_int32.h:27
+    NTT_R4(LENGTH, MODULUS, ROOT)                                    src/ntt_r4.h:30
+    NTT_R8(MODULUS, LENGTH, ROOT)                                    src/ntt_r8.h:22
+    BITREVERSE(LENGTH)                                               src/standalone_units.h:17
+    FULL_BARRETT_MULTIPLICATION(LENGTH, MODULUS, FACTOR)             src/standalone_units.h:40
+
+and ``dut_for_config(NTT_CONFIG)`` selects a design like src/project.cpp:139-157.
+The in_data / out_data ports become device buffers (torch tensors or raw
+pointers); ``run(iterations)`` transforms that many polynomials in one launch.
+The compute path is the CUDA library only: importing this module fails loudly
+when libgb300ntt.so is missing or cannot be loaded.
+"""
+import ctypes
+import enum
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libgb300ntt.so")
+
+
+class Kind(enum.IntEnum):
+    R2_I16_FWD = 0
+    R2_I16_INV = 1
+    R4_I16_FWD = 2
+    R8_I16_STAGE = 3
+    R2_I32_FWD = 4
+    R2_I32_INV = 5
+    BITREV_I16 = 6
+    FULL_BARRETT_I16 = 7
+    R8_I16_FWD = 8
+    R4_I16_INV = 9
+
+
+FLAG_CANONICAL = 0x1
+FLAG_R8_EXACT = 0x2
+FLAG_R8_FLOAT = 0x4
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported length", 3: "invalid modulus",
+          4: "root of unity has the wrong order", 5: "radix-4 needs an even number of layers",
+          6: "unknown design kind", 7: "CUDA error", 8: "out of memory", 9: "timeout",
+          10: "admission refused"}
+
+
+class NTTError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """The loaded libgb300ntt.so (raises if it is not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with "
+                              "`python -m ntts_on_amd_ai_engines_aie1_gb300.build`")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, u32, u64, i64, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int
+        L.gbntt_plan_create.argtypes = [ctypes.POINTER(vp), i32, u32, i64, i64, i64, u32]
+        L.gbntt_plan_destroy.argtypes = [vp]
+        L.gbntt_execute.argtypes = [vp, vp, vp, u64, vp]
+        L.gbntt_execute_host.argtypes = [vp, vp, vp, u64, vp]
+        L.gbntt_plan_query.argtypes = [vp, i32, ctypes.POINTER(i64)]
+        L.gbntt_host_tables.argtypes = [i32, u32, i64, i64, i64, u32, i32, ctypes.POINTER(i64), i64,
+                                        ctypes.POINTER(i64)]
+        L.gbntt_launch_count.restype = u64
+        L.gbntt_last_error.restype = ctypes.c_char_p
+        L.gbntt_status_string.restype = ctypes.c_char_p
+        L.gbntt_status_string.argtypes = [i32]
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise NTTError(rc, lib().gbntt_last_error().decode())
+
+
+def launch_count():
+    """Kernels launched by the library so far in this process."""
+    return int(lib().gbntt_launch_count())
+
+
+def host_tables(kind, n, q=0, root=0, factor=0, flags=0, which=0):
+    """The plan's host-side table (no CUDA call): which=0 (tw, w') pairs, 1 constants, 2 F8."""
+    import numpy as np
+    ln = ctypes.c_int64(0)
+    _check(lib().gbntt_host_tables(int(kind), n, q, root, factor, flags, which, None, 0, ctypes.byref(ln)))
+    out = np.zeros(ln.value, dtype=np.int64)
+    _check(lib().gbntt_host_tables(int(kind), n, q, root, factor, flags, which,
+                                   out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), ln.value,
+                                   ctypes.byref(ln)))
+    return out
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    return x.data_ptr()
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+class Plan:
+    """One design instance: tables built once and kept on the device."""
+
+    def __init__(self, kind, n, q=0, root=0, factor=0, flags=0):
+        h = ctypes.c_void_p()
+        _check(lib().gbntt_plan_create(ctypes.byref(h), int(kind), n, q, root, factor, flags))
+        self._h = h
+        self.kind, self.n, self.q, self.root, self.factor, self.flags = Kind(kind), n, q, root, factor, flags
+        self.elem_bytes = self.query(2)
+        self.stages = self.query(3)
+
+    @property
+    def handle(self):
+        return self._h.value
+
+    def query(self, what):
+        v = ctypes.c_int64(0)
+        _check(lib().gbntt_plan_query(self._h, what, ctypes.byref(v)))
+        return v.value
+
+    @property
+    def dtype(self):
+        import torch
+        return torch.int32 if self.elem_bytes == 4 else torch.int16
+
+    def execute(self, d_in, d_out, batch, stream=None):
+        """Raw-pointer launch (device buffers)."""
+        _check(lib().gbntt_execute(self._h, _ptr(d_in), _ptr(d_out), batch, _stream_ptr(stream)))
+
+    def __call__(self, x, out=None, stream=None):
+        """Transforms a (batch, n) or (n,) device tensor; returns the output tensor."""
+        import torch
+        if not x.is_cuda or x.dtype != self.dtype or not x.is_contiguous():
+            raise NTTError(1, f"input must be a contiguous CUDA {self.dtype} tensor")
+        if x.numel() % self.n:
+            raise NTTError(1, "input size is not a multiple of n")
+        if out is None:
+            out = torch.empty_like(x)
+        self.execute(x, out, x.numel() // self.n, stream)
+        return out
+
+    def execute_host(self, h_in, h_out, batch=None, stream=None):
+        """Host buffers (numpy arrays or torch CPU tensors); synchronous."""
+        def p(a):
+            return a.ctypes.data if hasattr(a, "ctypes") else a.data_ptr()
+        nb = batch if batch is not None else (h_in.size if hasattr(h_in, "size") and not callable(h_in.size)
+                                              else h_in.numel()) // self.n
+        _check(lib().gbntt_execute_host(self._h, p(h_in), p(h_out), nb, _stream_ptr(stream)))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().gbntt_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# mirrors of the reference graph classes
+# ---------------------------------------------------------------------------
+
+class NTT_TYPE(enum.Enum):
+    TYPE_NTT_NO_to_BO = 0     # forward, natural -> bit-reversed (src/ntt.h:31)
+    TYPE_INTT_BO_to_NO = 1    # inverse, bit-reversed -> natural (src/ntt.h:32)
+
+
+class NTT_INT32_TYPE(enum.Enum):
+    FORWARD_CT_NO_TO_BO = 0   # src/ntt_int32.h:20
+    INVERSE_GS_BO_TO_NO = 1   # src/ntt_int32.h:21
+
+
+class NTT_R4_TYPE(enum.Enum):
+    FORWARD_CT_NO_TO_BO = 0   # src/ntt_r4.h:24
+    INVERSE_BO_TO_NO = 1      # src/ntt_r4.h:18-20 (bit-reversal + forward with inverse twiddles)
+
+
+class _Graph:
+    """graph.init(); graph.run(N); graph.end() over device in/out ports."""
+
+    def __init__(self, kind, length, modulus=0, root=0, factor=0, flags=0):
+        self._args = (kind, length, modulus, root, factor, flags)
+        self.plan = None
+        self.in_data = None
+        self.out_data = None
+
+    @property
+    def NTT_LENGTH(self):
+        return self._args[1]
+
+    def init(self):
+        if self.plan is None:
+            self.plan = Plan(*self._args)
+        return self
+
+    def run(self, iterations=1, in_data=None, out_data=None, stream=None):
+        self.init()
+        src = in_data if in_data is not None else self.in_data
+        dst = out_data if out_data is not None else self.out_data
+        if dst is None:
+            import torch
+            dst = torch.empty_like(src)
+            self.out_data = dst
+        self.plan.execute(src, dst, iterations, stream)
+        return dst
+
+    def end(self):
+        if self.plan is not None:
+            self.plan.close()
+            self.plan = None
+
+
+class NTT(_Graph):
+    """Radix-2 int16 pipeline (src/ntt.h:43), forward or inverse."""
+
+    def __init__(self, LENGTH, MODULUS, ROOT, TYPE=NTT_TYPE.TYPE_NTT_NO_to_BO, flags=0):
+        kind = Kind.R2_I16_FWD if TYPE == NTT_TYPE.TYPE_NTT_NO_to_BO else Kind.R2_I16_INV
+        super().__init__(kind, LENGTH, MODULUS, ROOT, 0, flags)
+
+
+class NTT_INT32(_Graph):
+    """Radix-2 int32 pipeline (src/ntt_int32.h:27)."""
+
+    def __init__(self, LENGTH, MODULUS, ROOT, TYPE=NTT_INT32_TYPE.FORWARD_CT_NO_TO_BO, flags=0):
+        kind = Kind.R2_I32_FWD if TYPE == NTT_INT32_TYPE.FORWARD_CT_NO_TO_BO else Kind.R2_I32_INV
+        super().__init__(kind, LENGTH, MODULUS, ROOT, 0, flags)
+
+
+class NTT_R4(_Graph):
+    """Radix-4 int16 pipeline (src/ntt_r4.h:30)."""
+
+    def __init__(self, LENGTH, MODULUS, ROOT, TYPE=NTT_R4_TYPE.FORWARD_CT_NO_TO_BO, flags=0):
+        kind = Kind.R4_I16_FWD if TYPE == NTT_R4_TYPE.FORWARD_CT_NO_TO_BO else Kind.R4_I16_INV
+        super().__init__(kind, LENGTH, MODULUS, ROOT, 0, flags)
+
+
+class NTT_R8(_Graph):
+    """Radix-8 int16 (src/ntt_r8.h:22).  stages="one" is the reference graph
+    (one stage, float multipliers); stages="all" chains every stage."""
+
+    def __init__(self, MODULUS, LENGTH, ROOT, stages="one", flags=0):
+        kind = Kind.R8_I16_STAGE if stages == "one" else Kind.R8_I16_FWD
+        super().__init__(kind, LENGTH, MODULUS, ROOT, 0, flags)
+
+
+class BITREVERSE(_Graph):
+    """Bit-reversal unit (src/standalone_units.h:17; n in 256..4096 there)."""
+
+    def __init__(self, LENGTH):
+        super().__init__(Kind.BITREV_I16, LENGTH)
+
+
+class FULL_BARRETT_MULTIPLICATION(_Graph):
+    """out = FACTOR * in mod q in [0, q] (src/standalone_units.h:40)."""
+
+    def __init__(self, LENGTH, MODULUS, FACTOR):
+        super().__init__(Kind.FULL_BARRETT_I16, LENGTH, MODULUS, 0, FACTOR)
+
+
+# parameters of src/project.cpp:47-51
+Q_INT16, ROOT_INT16 = 12289, 41
+Q_INT32, ROOT_INT32 = 1073707009, 992735929
+BITREV_N = 4096
+
+
+def dut_for_config(NTT_CONFIG, BITREV_N=BITREV_N):
+    """The design under test of src/project.cpp:139-157 for NTT_CONFIG 0..7."""
+    if NTT_CONFIG == 0:
+        return NTT(4096, Q_INT16, ROOT_INT16, NTT_TYPE.TYPE_NTT_NO_to_BO)
+    if NTT_CONFIG == 1:
+        return NTT(4096, Q_INT16, ROOT_INT16, NTT_TYPE.TYPE_INTT_BO_to_NO)
+    if NTT_CONFIG == 2:
+        return NTT_R4(4096, Q_INT16, ROOT_INT16)
+    if NTT_CONFIG == 3:
+        return NTT_R8(Q_INT16, 4096, ROOT_INT16)
+    if NTT_CONFIG == 4:
+        return NTT_INT32(2048, Q_INT32, ROOT_INT32, NTT_INT32_TYPE.FORWARD_CT_NO_TO_BO)
+    if NTT_CONFIG == 5:
+        return NTT_INT32(2048, Q_INT32, ROOT_INT32, NTT_INT32_TYPE.INVERSE_GS_BO_TO_NO)
+    if NTT_CONFIG == 6:
+        return BITREVERSE(BITREV_N)
+    if NTT_CONFIG == 7:
+        return FULL_BARRETT_MULTIPLICATION(4096, Q_INT16, pow(4096, -1, Q_INT16))
+    raise ValueError("Unknown NTT_CONFIG, see the table at the top of src/project.cpp")

@@ -1,0 +1,283 @@
+// abi.cu -- the C ABI of libgb300ntt.so (declared in include/gb300_ntt.h).
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "../../include/gb300_ntt.h"
+#include "device.cuh"
+#include "tables.h"
+
+namespace gbntt {
+const void* bitrev_kernel_ptr();
+}
+
+using namespace gbntt;
+
+struct gbntt_plan {
+    HostPlan hp;
+    int fam = -1;          // transform family of k_ntt, -1 for the single-purpose kernels
+    bool br = false;       // bit-reversed load and store (radix-4 inverse)
+    KernelInfo ki;
+    KArgs base;            // constants shared by every launch
+    int2* d_tab = nullptr;
+    size_t tab_bytes = 0;
+    int device = 0;
+    std::mutex stage_mu;   // serialises gbntt_execute_host on this plan
+    void* d_stage = nullptr;
+    size_t stage_bytes = 0;
+};
+
+namespace {
+
+thread_local std::string g_err;
+std::atomic<unsigned long long> g_launches{0};
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return GBNTT_ERR_CUDA;
+}
+
+int family_of(int kind) {
+    switch (kind) {
+    case K_R2_I16_FWD: return F_R2F16;
+    case K_R2_I16_INV: return F_R2I16;
+    case K_R4_I16_FWD: return F_R4F16;
+    case K_R4_I16_INV: return F_R4F16;
+    case K_R8_I16_FWD: return F_R8F16;
+    case K_R2_I32_FWD: return F_R2F32;
+    case K_R2_I32_INV: return F_R2G32;
+    default: return -1;
+    }
+}
+
+KernelInfo kernel_for(int fam, int L, bool br) {
+    switch (fam) {
+    case F_R2F16: return kinfo_r2f16(L);
+    case F_R2I16: return kinfo_r2i16(L);
+    case F_R4F16: return kinfo_r4(L, br);
+    case F_R8F16: return kinfo_r8(L);
+    case F_R2F32: return kinfo_r2f32(L);
+    case F_R2G32: return kinfo_r2g32(L);
+    default: return KernelInfo();
+    }
+}
+
+int launch(const gbntt_plan* p, const void* d_in, void* d_out, uint64_t batch, cudaStream_t s) {
+    KArgs a = p->base;
+    a.in = d_in;
+    a.out = d_out;
+    a.batch = (long long)batch;
+    cudaError_t e = cudaSuccess;
+    if (p->fam >= 0) {
+        const unsigned long long blocks = (batch + p->ki.polys - 1) / p->ki.polys;
+        if (blocks > 0x7FFFFFFFull) return fail(GBNTT_ERR_ARG, "batch too large for one launch");
+        void* args[] = {&a};
+        e = cudaLaunchKernel(p->ki.fn, dim3((unsigned)blocks), dim3(p->ki.threads), args, p->ki.smem, s);
+    } else if (p->hp.kind == K_R8_I16_STAGE) {
+        e = launch_r8_stage(a, p->hp.L, s);
+    } else if (p->hp.kind == K_BITREV_I16) {
+        e = launch_bitrev(a, p->hp.L, s);
+    } else if (p->hp.kind == K_FULL_BARRETT_I16) {
+        e = launch_full_barrett(a, (long long)batch * p->hp.n, p->hp.fb_fs, p->hp.fb_wq, s);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return GBNTT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbntt_abi_version(void) { return GBNTT_ABI_VERSION; }
+
+const char* gbntt_last_error(void) { return g_err.c_str(); }
+
+uint64_t gbntt_launch_count(void) { return g_launches.load(); }
+
+const char* gbntt_status_string(int status) {
+    switch (status) {
+    case GBNTT_OK: return "ok";
+    case GBNTT_ERR_ARG: return "invalid argument";
+    case GBNTT_ERR_LENGTH: return "unsupported length";
+    case GBNTT_ERR_MODULUS: return "invalid modulus";
+    case GBNTT_ERR_ROOT: return "root of unity has the wrong order";
+    case GBNTT_ERR_LAYERS: return "radix-4 needs an even number of layers";
+    case GBNTT_ERR_KIND: return "unknown design kind";
+    case GBNTT_ERR_CUDA: return "CUDA error";
+    case GBNTT_ERR_NOMEM: return "out of memory";
+    case GBNTT_ERR_TIMEOUT: return "timeout";
+    case GBNTT_ERR_ADMISSION: return "admission refused";
+    default: return "unknown status";
+    }
+}
+
+int gbntt_host_tables(int kind, uint32_t n, int64_t q, int64_t root, int64_t factor, uint32_t flags,
+                      int which, int64_t* dst, int64_t cap, int64_t* len) {
+    HostPlan hp;
+    std::string err;
+    const int rc = build_host_plan(kind, n, q, root, factor, flags, hp, err);
+    if (rc != GBNTT_OK) return fail(rc, err);
+    std::vector<int64_t> v;
+    if (which == 0) {
+        v.assign(hp.tab.begin(), hp.tab.end());
+    } else if (which == 1) {
+        v = {hp.c, hp.r4_fneg, hp.r4_wc, hp.fb_fs, hp.fb_wq, hp.tail_wq, hp.tail_bits, hp.r8_sym, hp.stages};
+    } else if (which == 2) {
+        v.assign(hp.f8, hp.f8 + 64);
+    } else {
+        return fail(GBNTT_ERR_ARG, "unknown table selector");
+    }
+    if (len) *len = (int64_t)v.size();
+    if (dst)
+        for (int64_t i = 0; i < (int64_t)v.size() && i < cap; ++i) dst[i] = v[i];
+    return GBNTT_OK;
+}
+
+int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t root, int64_t factor,
+                      uint32_t flags) {
+    if (!out) return fail(GBNTT_ERR_ARG, "plan pointer is null");
+    *out = nullptr;
+    gbntt_plan* p = new (std::nothrow) gbntt_plan();
+    if (!p) return fail(GBNTT_ERR_NOMEM, "host allocation failed");
+    std::string err;
+    int rc = build_host_plan(kind, n, q, root, factor, flags, p->hp, err);
+    if (rc != GBNTT_OK) {
+        delete p;
+        return fail(rc, err);
+    }
+    const HostPlan& hp = p->hp;
+    p->fam = family_of(kind);
+    p->br = (kind == K_R4_I16_INV);
+    if (p->fam >= 0) {
+        p->ki = kernel_for(p->fam, hp.L, p->br);
+        if (!p->ki.fn) {
+            delete p;
+            return fail(GBNTT_ERR_LENGTH, "no kernel for this length");
+        }
+    }
+    cudaError_t e = cudaGetDevice(&p->device);
+    if (e != cudaSuccess) {
+        delete p;
+        return cuda_fail(e, "cudaGetDevice");
+    }
+    if (p->fam >= 0 && p->ki.smem > 48 * 1024) {
+        e = cudaFuncSetAttribute(p->ki.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, p->ki.smem);
+        if (e != cudaSuccess) {
+            delete p;
+            return cuda_fail(e, "cudaFuncSetAttribute");
+        }
+    }
+    if (kind == K_BITREV_I16 && bitrev_smem_bytes(hp.L) > 48 * 1024) {
+        e = cudaFuncSetAttribute(bitrev_kernel_ptr(), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 bitrev_smem_bytes(hp.L));
+        if (e != cudaSuccess) {
+            delete p;
+            return cuda_fail(e, "cudaFuncSetAttribute");
+        }
+    }
+    if (!hp.tab.empty()) {
+        p->tab_bytes = hp.tab.size() * sizeof(int32_t);
+        e = cudaMalloc(&p->d_tab, p->tab_bytes);
+        if (e != cudaSuccess) {
+            delete p;
+            return e == cudaErrorMemoryAllocation ? fail(GBNTT_ERR_NOMEM, "device allocation failed")
+                                                  : cuda_fail(e, "cudaMalloc");
+        }
+        e = cudaMemcpy(p->d_tab, hp.tab.data(), p->tab_bytes, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(p->d_tab);
+            delete p;
+            return cuda_fail(e, "cudaMemcpy (tables)");
+        }
+    }
+    KArgs& a = p->base;
+    std::memset(&a, 0, sizeof(a));
+    a.tab = p->d_tab;
+    a.q = (int)hp.q;
+    a.c = hp.c;
+    a.fneg = hp.r4_fneg;
+    a.wc = hp.r4_wc;
+    a.canonical = (flags & FLAG_CANONICAL) ? 1 : 0;
+    a.r8_sym = hp.r8_sym;
+    a.tail_wq = hp.tail_wq;
+    for (int i = 0; i < 64; ++i) a.f8[i] = hp.f8[i];
+    for (int i = 0; i < 4; ++i) a.f8s[i] = hp.f8s[i];
+    for (int i = 0; i < 16; ++i) a.ftail[i] = hp.ftail[i];
+    *out = p;
+    return GBNTT_OK;
+}
+
+int gbntt_plan_destroy(gbntt_plan* p) {
+    if (!p) return GBNTT_OK;
+    if (p->d_tab) cudaFree(p->d_tab);
+    if (p->d_stage) cudaFree(p->d_stage);
+    delete p;
+    return GBNTT_OK;
+}
+
+int gbntt_plan_query(const gbntt_plan* p, int what, int64_t* value) {
+    if (!p || !value) return fail(GBNTT_ERR_ARG, "null argument");
+    switch (what) {
+    case GBNTT_Q_N: *value = p->hp.n; break;
+    case GBNTT_Q_MODULUS: *value = p->hp.q; break;
+    case GBNTT_Q_ELEM_BYTES: *value = p->hp.elem_bytes; break;
+    case GBNTT_Q_STAGES: *value = p->hp.stages; break;
+    case GBNTT_Q_KIND: *value = p->hp.kind; break;
+    case GBNTT_Q_TABLE_BYTES: *value = (int64_t)p->tab_bytes; break;
+    default: return fail(GBNTT_ERR_ARG, "unknown query");
+    }
+    return GBNTT_OK;
+}
+
+int gbntt_execute(const gbntt_plan* p, const void* d_in, void* d_out, uint64_t batch, void* stream) {
+    if (!p) return fail(GBNTT_ERR_ARG, "plan is null");
+    if (batch == 0) return GBNTT_OK;
+    if (!d_in || !d_out) return fail(GBNTT_ERR_ARG, "null buffer");
+    if ((reinterpret_cast<uintptr_t>(d_in) | reinterpret_cast<uintptr_t>(d_out)) & 15)
+        return fail(GBNTT_ERR_ARG, "device buffers must be 16-byte aligned");
+    if (p->hp.kind == K_R8_I16_STAGE && d_in == d_out)
+        return fail(GBNTT_ERR_ARG, "the radix-8 stage cannot run in place");
+    return launch(p, d_in, d_out, batch, static_cast<cudaStream_t>(stream));
+}
+
+int gbntt_execute_host(gbntt_plan* p, const void* h_in, void* h_out, uint64_t batch, void* stream) {
+    if (!p) return fail(GBNTT_ERR_ARG, "plan is null");
+    if (batch == 0) return GBNTT_OK;
+    if (!h_in || !h_out) return fail(GBNTT_ERR_ARG, "null buffer");
+    std::lock_guard<std::mutex> lock(p->stage_mu);
+    const size_t bytes = (size_t)batch * p->hp.n * (size_t)p->hp.elem_bytes;
+    // the radix-8 stage reads other threads' outputs, so it gets its own output half
+    const bool split = (p->hp.kind == K_R8_I16_STAGE);
+    const size_t need = split ? 2 * bytes : bytes;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e;
+    if (p->stage_bytes < need) {
+        if (p->d_stage) cudaFree(p->d_stage);
+        p->d_stage = nullptr;
+        p->stage_bytes = 0;
+        e = cudaMalloc(&p->d_stage, need);
+        if (e != cudaSuccess) return fail(GBNTT_ERR_NOMEM, "staging allocation failed");
+        p->stage_bytes = need;
+    }
+    void* d_out = split ? static_cast<char*>(p->d_stage) + bytes : p->d_stage;
+    e = cudaMemcpyAsync(p->d_stage, h_in, bytes, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync H2D");
+    int rc = launch(p, p->d_stage, d_out, batch, s);
+    if (rc != GBNTT_OK) return rc;
+    e = cudaMemcpyAsync(h_out, d_out, bytes, cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync D2H");
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    return GBNTT_OK;
+}
+
+}  // extern "C"

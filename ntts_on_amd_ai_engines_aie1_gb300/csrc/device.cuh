@@ -1,0 +1,481 @@
+// device.cuh -- sm_103a device code of the GB300 NTT library.
+//
+// The reference runs one radix-2 (radix-4, radix-8) layer per AIE tile in
+// constant geometry (Pease): every tile reads positions j and j + n/2 and
+// writes 2j, 2j + 1.  Constant geometry only moves data between tiles; the
+// arithmetic of every butterfly is fixed by which values meet, with which
+// twiddle, and where the partial Barrett reductions sit.  These kernels
+// therefore run the same butterflies in place, in registers: a group of G
+// threads owns one polynomial of n = 2^L coefficients, each thread holds
+// E = 2^EL of them, and a "window" of EL position bits is resident in each
+// thread at a time.  All layers whose butterfly bits lie in the window run in
+// registers; between windows the polynomial is exchanged through shared
+// memory.  The values computed are bit-identical to the reference's:
+//   * partial Barrett with K = 16 / 32 / 31 and rounding of the SRS unit in
+//     symmetric_zero mode (nearest, ties toward zero);
+//   * int16 / int32 two's-complement wrap wherever the AIE code stores to
+//     int16 / int32 lanes (saturation mode none).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <utility>
+
+namespace gbntt {
+
+enum Fam { F_R2F16 = 0, F_R2I16 = 1, F_R4F16 = 2, F_R8F16 = 3, F_R2F32 = 4, F_R2G32 = 5, F_NUM = 6 };
+
+// Per-launch arguments (by value; the kernel reads the constants from the
+// parameter bank).
+struct KArgs {
+    const void* in;
+    void* out;
+    long long batch;
+    const int2* tab;      // (tw, w') pairs of the design
+    int q;
+    int c;                // Barrett constant of the reduction (K = 16 or 32)
+    int fneg, wc;         // radix-4 omega_4 and its multiplier
+    int canonical;        // reduce outputs to [0, q)
+    int r8_sym;           // radix-8 matrix symmetric: use the factored butterfly
+    int tail_wq;          // radix-8 tail stage multiplier of the twiddle 1
+    int f8[64];           // radix-8 matrix [m][k]
+    int f8s[4];           // f1, f2, f3
+    int ftail[16];        // tail matrix [m][k]
+};
+
+// ---------------------------------------------------------------------------
+// lane arithmetic
+// ---------------------------------------------------------------------------
+
+// round(p / 2^16), ties toward zero (SRS, symmetric_zero)
+__device__ __forceinline__ int rsz16(int p) { return (p + 0x7FFF + (int)((unsigned)p >> 31)) >> 16; }
+
+// round(p / 2^32), ties toward zero
+__device__ __forceinline__ int rsz32(long long p) {
+    return (int)((p + 0x7FFFFFFFLL + (long long)((unsigned long long)p >> 63)) >> 32);
+}
+
+// round(p / 2^31), ties toward zero
+__device__ __forceinline__ int rsz31(long long p) {
+    return (int)((p + 0x3FFFFFFFLL + (long long)((unsigned long long)p >> 63)) >> 31);
+}
+
+__device__ __forceinline__ int wrap16(int x) { return (int)(short)x; }
+
+// partial Barrett reduction, int16: a - round(a c / 2^16) q
+__device__ __forceinline__ int br16(int a, int c, int q) { return wrap16(a - rsz16(a * c) * q); }
+// partial Barrett multiplication, int16: a w - round(a w' / 2^16) q
+__device__ __forceinline__ int bm16(int a, int tw, int wq, int q) { return wrap16(a * tw - rsz16(a * wq) * q); }
+
+// int32 variants, computed modulo 2^32 like the int32 lanes
+__device__ __forceinline__ int br32(int a, int c, int q) {
+    return (int)((unsigned)a - (unsigned)rsz32((long long)a * c) * (unsigned)q);
+}
+__device__ __forceinline__ int bm32(int a, int tw, int wq, int q) {
+    return (int)((unsigned)a * (unsigned)tw - (unsigned)rsz32((long long)a * wq) * (unsigned)q);
+}
+__device__ __forceinline__ int add32(int a, int b) { return (int)((unsigned)a + (unsigned)b); }
+__device__ __forceinline__ int sub32(int a, int b) { return (int)((unsigned)a - (unsigned)b); }
+
+// radix-8 reduction tile: m' = round(y w' / 2^31) truncated to int16, then
+// y w - m' q kept as int16 (ntt_r8_kernels.cc:30-177)
+__device__ __forceinline__ int r8red(int y, int tw, int wq, int q) {
+    const int m16 = (int)(short)rsz31((long long)y * wq);
+    return wrap16((int)((unsigned)y * (unsigned)tw - (unsigned)m16 * (unsigned)q));
+}
+
+// x mod q in [0, q)
+__device__ __forceinline__ int canon(int x, int q) {
+    int r = x % q;
+    return r < 0 ? r + q : r;
+}
+
+// ---------------------------------------------------------------------------
+// compile-time schedule
+// ---------------------------------------------------------------------------
+
+__host__ __device__ constexpr bool fam_i32(int fam) { return fam == F_R2F32 || fam == F_R2G32; }
+// forward designs consume position bits from the top, inverse ones from the bottom
+__host__ __device__ constexpr bool topdown(int fam) { return fam != F_R2I16 && fam != F_R2G32; }
+__host__ __device__ constexpr int nsteps(int fam, int L) {
+    return fam == F_R4F16 ? L / 2 : fam == F_R8F16 ? L / 3 + (L % 3 ? 1 : 0) : L;
+}
+__host__ __device__ constexpr int step_w(int fam, int L, int s) {
+    return fam == F_R4F16 ? 2 : fam == F_R8F16 ? (s < L / 3 ? 3 : L % 3) : 1;
+}
+__host__ __device__ constexpr int step_b(int fam, int L, int s) {
+    return fam == F_R4F16 ? L - 2 - 2 * s
+         : fam == F_R8F16 ? (s < L / 3 ? L - 3 - 3 * s : 0)
+         : topdown(fam) ? L - 1 - s : s;
+}
+// lowest position bit of the register window used by step s
+__host__ __device__ constexpr int window_lo(int fam, int L, int EL, int s) {
+    int lo = topdown(fam) ? L - EL : 0;
+    for (int i = 0; i <= s; ++i) {
+        const int b = step_b(fam, L, i), w = step_w(fam, L, i);
+        if (b < lo || b + w > lo + EL)
+            lo = topdown(fam) ? (b + w - EL < 0 ? 0 : b + w - EL) : (b > L - EL ? L - EL : b);
+    }
+    return lo;
+}
+__host__ __device__ constexpr int num_windows(int fam, int L, int EL) {
+    int c = 1;
+    for (int s = 1; s < nsteps(fam, L); ++s)
+        if (window_lo(fam, L, EL, s) != window_lo(fam, L, EL, s - 1)) ++c;
+    return c;
+}
+
+// first table entry of radix-8 stage s (8 * 2^(L-3-3t) entries per stage t)
+__host__ __device__ constexpr int r8_stage_offset(int L, int s) {
+    int o = 0;
+    for (int t = 0; t < s; ++t) o += 8 << (L - 3 - 3 * t);
+    return o;
+}
+
+// padded shared-memory index of a position (one spare word every 32)
+__device__ __forceinline__ int spad(int pos) { return pos + (pos >> 5); }
+
+// position of register k of thread g when the window starts at bit LO
+template <int LO, int EL>
+__device__ __forceinline__ int posmap(int g, int k) {
+    return ((g >> LO) << (LO + EL)) | (k << LO) | (g & ((1 << LO) - 1));
+}
+
+template <int G>
+__device__ __forceinline__ void group_sync() {
+    if constexpr (G > 32) __syncthreads();
+    else __syncwarp();
+}
+
+template <int NB>
+__host__ __device__ constexpr int brev_c(int x) {
+    int r = 0;
+    for (int i = 0; i < NB; ++i) r |= ((x >> i) & 1) << (NB - 1 - i);
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// butterflies of one step (all groups of the thread's window)
+// ---------------------------------------------------------------------------
+
+template <int FAM, int L, int EL, int S>
+__device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const KArgs& a) {
+    constexpr int E = 1 << EL;
+    constexpr int G = 1 << (L - EL);
+    constexpr int LO = window_lo(FAM, L, EL, S);
+    constexpr int B = step_b(FAM, L, S);
+    constexpr int W = step_w(FAM, L, S);
+    constexpr int KB = B - LO;
+    static_assert(B >= LO && B + W <= LO + EL, "step outside its window");
+    if constexpr (S > 0) {
+        constexpr int PLO = window_lo(FAM, L, EL, S - 1);
+        if constexpr (PLO != LO) {
+            group_sync<G>();
+#pragma unroll
+            for (int k = 0; k < E; ++k) sp[spad(posmap<PLO, EL>(g, k))] = v[k];
+            group_sync<G>();
+#pragma unroll
+            for (int k = 0; k < E; ++k) v[k] = sp[spad(posmap<LO, EL>(g, k))];
+        }
+    }
+    const int q = a.q;
+#pragma unroll
+    for (int r = 0; r < (E >> W); ++r) {
+        const int k0 = ((r >> KB) << (KB + W)) | (r & ((1 << KB) - 1));
+        if constexpr (FAM == F_R2F16 || FAM == F_R2F32) {
+            // forward CT layer S: block = position bits above B (src/kernels/
+            // ntt_r2_kernels.cc:434-472, ntt_r2_int32_kernels.cc:267-295)
+            const int k1 = k0 | (1 << KB);
+            const int blk = posmap<LO, EL>(g, k0) >> (B + 1);
+            const int2 t = __ldg(&a.tab[blk]);
+            if constexpr (FAM == F_R2F16) {
+                const int u = br16(v[k0], a.c, q), w = bm16(v[k1], t.x, t.y, q);
+                v[k0] = wrap16(u + w);
+                v[k1] = wrap16(u - w);
+            } else {
+                const int u = br32(v[k0], a.c, q), w = bm32(v[k1], t.x, t.y, q);
+                v[k0] = add32(u, w);
+                v[k1] = sub32(u, w);
+            }
+        } else if constexpr (FAM == F_R2G32) {
+            // inverse GS layer S (ntt_r2_int32_kernels.cc:305-336)
+            const int k1 = k0 | (1 << KB);
+            const int blk = posmap<LO, EL>(g, k0) >> (B + 1);
+            const int2 t = __ldg(&a.tab[blk]);
+            const int s = add32(v[k0], v[k1]), d = sub32(v[k0], v[k1]);
+            v[k0] = br32(s, a.c, q);
+            v[k1] = bm32(d, t.x, t.y, q);
+        } else if constexpr (FAM == F_R2I16) {
+            // inverse CT layer S on bit-reversed input (ntt_r2_kernels.cc:484-540)
+            const int k1 = k0 | (1 << KB);
+            if constexpr (S == 0) {
+                const int s = wrap16(v[k0] + v[k1]), d = wrap16(v[k0] - v[k1]);
+                v[k0] = s;
+                v[k1] = d;
+            } else {
+                const int tpos = posmap<LO, EL>(g, k0) & ((1 << B) - 1);
+                const int2 t = __ldg(&a.tab[(1 << B) + tpos]);
+                const int u = br16(v[k0], a.c, q), w = bm16(v[k1], t.x, t.y, q);
+                v[k0] = wrap16(u + w);
+                v[k1] = wrap16(u - w);
+            }
+        } else if constexpr (FAM == F_R4F16) {
+            // radix-4 layer S (ntt_r4_kernels.cc:243-261)
+            constexpr int OFF = 4 * (((1 << (2 * S)) - 1) / 3);
+            const int blk = posmap<LO, EL>(g, k0) >> (B + 2);
+            const int4* t4 = reinterpret_cast<const int4*>(a.tab + OFF + 4 * blk);
+            const int4 t01 = __ldg(t4), t23 = __ldg(t4 + 1);
+            const int ka = k0, kb1 = k0 | (1 << KB), kb2 = k0 | (2 << KB), kb3 = k0 | (3 << KB);
+            const int A0 = bm16(v[ka], t01.x, t01.y, q);
+            const int A1 = bm16(v[kb1], t01.z, t01.w, q);
+            const int A2 = bm16(v[kb2], t23.x, t23.y, q);
+            const int A3 = bm16(v[kb3], t23.z, t23.w, q);
+            const int A5 = bm16(A1, a.fneg, a.wc, q);
+            const int A6 = bm16(A3, a.fneg, a.wc, q);
+            v[ka] = wrap16(A0 + A1 + A2 + A3);
+            v[kb1] = wrap16(A0 - A1 + A2 - A3);    // y2 -> digit bitrev2(2) = 1
+            v[kb2] = wrap16(A0 + A5 - A2 - A6);    // y1 -> digit 2
+            v[kb3] = wrap16(A0 - A5 - A2 + A6);    // y3 -> digit 3
+        } else if constexpr (FAM == F_R8F16) {
+            if constexpr (W == 3) {
+                // radix-8 stage S: y = x F8 (int32), then the reduction tile
+                // with twiddle root^(8^S r k) (ntt_r8_kernels.cc:30-404)
+                constexpr int OFF = r8_stage_offset(L, S);
+                const int rr = posmap<LO, EL>(g, k0) & ((1 << B) - 1);
+                int x[8], y[8];
+#pragma unroll
+                for (int m = 0; m < 8; ++m) x[m] = v[k0 | (m << KB)];
+                if (a.r8_sym) {
+                    const int f1 = a.f8s[1], f2 = a.f8s[2], f3 = a.f8s[3];
+                    const int a0 = x[0] + x[4], a1 = x[1] + x[5], a2 = x[2] + x[6], a3 = x[3] + x[7];
+                    const int b0 = x[0] - x[4], b1 = x[1] - x[5], b2 = x[2] - x[6], b3 = x[3] - x[7];
+                    const int c0 = a0 + a2, c1 = a1 + a3, d0 = a0 - a2, d1 = a1 - a3;
+                    y[0] = c0 + c1;
+                    y[4] = c0 - c1;
+                    const int t2 = f2 * d1;
+                    y[2] = d0 + t2;
+                    y[6] = d0 - t2;
+                    const int e0 = b0 + f2 * b2, e1 = b0 - f2 * b2;
+                    const int h1 = f1 * b1 + f3 * b3, h3 = f3 * b1 + f1 * b3;
+                    y[1] = e0 + h1;
+                    y[5] = e0 - h1;
+                    y[3] = e1 + h3;
+                    y[7] = e1 - h3;
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        int acc = 0;
+#pragma unroll
+                        for (int m = 0; m < 8; ++m) acc += x[m] * a.f8[8 * m + k];
+                        y[k] = acc;
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const int2 t = __ldg(&a.tab[OFF + (k << B) + rr]);
+                    v[k0 | (brev_c<3>(k) << KB)] = r8red(y[k], t.x, t.y, q);
+                }
+            } else {
+                // radix-2^W tail stage, twiddle 1
+                constexpr int R = 1 << W;
+                int x[R];
+#pragma unroll
+                for (int m = 0; m < R; ++m) x[m] = v[k0 | (m << KB)];
+#pragma unroll
+                for (int k = 0; k < R; ++k) {
+                    int acc = 0;
+#pragma unroll
+                    for (int m = 0; m < R; ++m) acc += x[m] * a.ftail[R * m + k];
+                    v[k0 | (brev_c<W>(k) << KB)] = r8red(acc, 1, a.tail_wq, q);
+                }
+            }
+        }
+    }
+}
+
+template <int FAM, int L, int EL, int... S>
+__device__ __forceinline__ void run_steps(int (&v)[1 << EL], int* sp, int g, const KArgs& a,
+                                          std::integer_sequence<int, S...>) {
+    (do_step<FAM, L, EL, S>(v, sp, g, a), ...);
+}
+
+// ---------------------------------------------------------------------------
+// load / store of one polynomial in a window layout
+// ---------------------------------------------------------------------------
+
+template <bool I32, int L, int EL, int LO, bool BR>
+__device__ __forceinline__ void load_poly(int (&v)[1 << EL], const KArgs& a, long long poly, int g) {
+    constexpr int E = 1 << EL;
+    constexpr long long N = 1LL << L;
+    if constexpr (I32) {
+        const int* src = static_cast<const int*>(a.in) + poly * N;
+        if constexpr (LO == 0 && !BR && E >= 4) {
+            const int4* s4 = reinterpret_cast<const int4*>(src + (long long)g * E);
+#pragma unroll
+            for (int j = 0; j < E / 4; ++j) {
+                const int4 w = __ldg(s4 + j);
+                v[4 * j] = w.x; v[4 * j + 1] = w.y; v[4 * j + 2] = w.z; v[4 * j + 3] = w.w;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < E; ++k) {
+                int p = posmap<LO, EL>(g, k);
+                if constexpr (BR) p = (int)(__brev((unsigned)p) >> (32 - L));
+                v[k] = __ldg(src + p);
+            }
+        }
+    } else {
+        const short* src = static_cast<const short*>(a.in) + poly * N;
+        if constexpr (LO == 0 && !BR && E >= 8) {
+            const int4* s4 = reinterpret_cast<const int4*>(src + (long long)g * E);
+#pragma unroll
+            for (int j = 0; j < E / 8; ++j) {
+                const int4 w = __ldg(s4 + j);
+                const int ww[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    v[8 * j + 2 * h] = (int)(short)(ww[h] & 0xFFFF);
+                    v[8 * j + 2 * h + 1] = ww[h] >> 16;
+                }
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < E; ++k) {
+                int p = posmap<LO, EL>(g, k);
+                if constexpr (BR) p = (int)(__brev((unsigned)p) >> (32 - L));
+                v[k] = (int)__ldg(src + p);
+            }
+        }
+    }
+}
+
+template <bool I32, int L, int EL, int LO, bool BR>
+__device__ __forceinline__ void store_poly(int (&v)[1 << EL], const KArgs& a, long long poly, int g) {
+    constexpr int E = 1 << EL;
+    constexpr long long N = 1LL << L;
+    if (a.canonical) {
+#pragma unroll
+        for (int k = 0; k < E; ++k) v[k] = canon(v[k], a.q);
+    }
+    if constexpr (I32) {
+        int* dst = static_cast<int*>(a.out) + poly * N;
+        if constexpr (LO == 0 && !BR && E >= 4) {
+            int4* d4 = reinterpret_cast<int4*>(dst + (long long)g * E);
+#pragma unroll
+            for (int j = 0; j < E / 4; ++j) d4[j] = make_int4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < E; ++k) {
+                int p = posmap<LO, EL>(g, k);
+                if constexpr (BR) p = (int)(__brev((unsigned)p) >> (32 - L));
+                dst[p] = v[k];
+            }
+        }
+    } else {
+        short* dst = static_cast<short*>(a.out) + poly * N;
+        if constexpr (LO == 0 && !BR && E >= 8) {
+            int4* d4 = reinterpret_cast<int4*>(dst + (long long)g * E);
+#pragma unroll
+            for (int j = 0; j < E / 8; ++j) {
+                int ww[4];
+#pragma unroll
+                for (int h = 0; h < 4; ++h)
+                    ww[h] = (v[8 * j + 2 * h] & 0xFFFF) | (v[8 * j + 2 * h + 1] << 16);
+                d4[j] = make_int4(ww[0], ww[1], ww[2], ww[3]);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < E; ++k) {
+                int p = posmap<LO, EL>(g, k);
+                if constexpr (BR) p = (int)(__brev((unsigned)p) >> (32 - L));
+                dst[p] = (short)v[k];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// the transform kernel: P polynomials per CTA, G = 2^(L-EL) threads each
+// ---------------------------------------------------------------------------
+
+template <int FAM, int L, int EL, int P, bool BR>
+__global__ void __launch_bounds__(P << (L - EL)) k_ntt(const KArgs a) {
+    constexpr int G = 1 << (L - EL);
+    constexpr int NS = nsteps(FAM, L);
+    constexpr int N = 1 << L;
+    constexpr int SW = N + N / 32;
+    constexpr bool I32 = fam_i32(FAM);
+    extern __shared__ int smem[];
+    const int tid = threadIdx.x;
+    const int lp = tid / G, g = tid % G;
+    const long long poly = (long long)blockIdx.x * P + lp;
+    const bool active = poly < a.batch;
+    int* sp = smem + lp * SW;
+    int v[1 << EL];
+    constexpr int LO0 = window_lo(FAM, L, EL, 0);
+    constexpr int LOZ = window_lo(FAM, L, EL, NS - 1);
+    if (active) {
+        load_poly<I32, L, EL, LO0, BR>(v, a, poly, g);
+    } else {
+#pragma unroll
+        for (int k = 0; k < (1 << EL); ++k) v[k] = 0;
+    }
+    run_steps<FAM, L, EL>(v, sp, g, a, std::make_integer_sequence<int, NS>{});
+    if (active) store_poly<I32, L, EL, LOZ, BR>(v, a, poly, g);
+}
+
+struct KernelInfo {
+    const void* fn = nullptr;
+    int threads = 0;
+    int smem = 0;
+    int polys = 0;
+    int el = 0;
+};
+
+// elements per thread (log2) and polynomials per CTA of each design
+__host__ __device__ constexpr int choose_el(int fam, int L) {
+    if (L <= 5) return L;
+    if (fam == F_R4F16) return (L <= 8) ? 4 : 6;
+    if (fam == F_R8F16) return 6;
+    return L <= 12 ? (L + 1) / 2 : 6;
+}
+__host__ __device__ constexpr int choose_polys(int fam, int L) {
+    const int G = 1 << (L - choose_el(fam, L));
+    const int p = 256 / G;
+    return p < 1 ? 1 : p;
+}
+__host__ __device__ constexpr int smem_bytes(int fam, int L) {
+    return num_windows(fam, L, choose_el(fam, L)) > 1
+               ? choose_polys(fam, L) * ((1 << L) + (1 << L) / 32) * 4
+               : 0;
+}
+
+template <int FAM, int L, bool BR>
+KernelInfo make_kernel_info() {
+    constexpr int EL = choose_el(FAM, L);
+    constexpr int P = choose_polys(FAM, L);
+    KernelInfo ki;
+    ki.fn = reinterpret_cast<const void*>(&k_ntt<FAM, L, EL, P, BR>);
+    ki.threads = P << (L - EL);
+    ki.smem = smem_bytes(FAM, L);
+    ki.polys = P;
+    ki.el = EL;
+    return ki;
+}
+
+// kernel tables, one per family (kernels_*.cu)
+KernelInfo kinfo_r2f16(int L);
+KernelInfo kinfo_r2i16(int L);
+KernelInfo kinfo_r2f32(int L);
+KernelInfo kinfo_r2g32(int L);
+KernelInfo kinfo_r4(int L, bool br);
+KernelInfo kinfo_r8(int L);
+
+// single-purpose kernels (kernels_misc.cu)
+cudaError_t launch_r8_stage(const KArgs& a, int L, cudaStream_t s);
+cudaError_t launch_bitrev(const KArgs& a, int L, cudaStream_t s);
+cudaError_t launch_full_barrett(const KArgs& a, long long total, int fs, int wq, cudaStream_t s);
+int bitrev_smem_bytes(int L);
+
+}  // namespace gbntt
+

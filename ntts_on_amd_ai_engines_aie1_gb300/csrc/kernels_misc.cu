@@ -1,0 +1,162 @@
+// kernels_misc.cu -- the single-pass designs: one radix-8 stage, the
+// bit-reversal unit and the full Barrett multiplication by a constant.
+#include "device.cuh"
+
+namespace gbntt {
+
+namespace {
+
+// One radix-8 stage exactly as the reference's NTT_R8 graph (butterfly tile
+// src/kernels/ntt_r8_kernels.cc:214-404 + reduction tile :30-177): thread t of
+// polynomial p reads x[i + M m] (M = n/8), forms y_k = sum_m x_m F8[m][k] in
+// int32, reduces y_k with twiddle root^(i k) and writes the eight results
+// (de-interleaved and 3-bit reversed, :152-154) as one 16-byte store at 8 i.
+__global__ void __launch_bounds__(256) k_r8_stage(const KArgs a, int L) {
+    const int n = 1 << L, M = n >> 3;
+    const long long total = a.batch << (L - 3);
+    const short* in = static_cast<const short*>(a.in);
+    short* out = static_cast<short*>(a.out);
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long poly = idx >> (L - 3);
+        const int i = (int)(idx & (M - 1));
+        const short* src = in + poly * n + i;
+        int x[8], y[8];
+#pragma unroll
+        for (int m = 0; m < 8; ++m) x[m] = __ldg(src + m * M);
+        if (a.r8_sym) {
+            const int f1 = a.f8s[1], f2 = a.f8s[2], f3 = a.f8s[3];
+            const int a0 = x[0] + x[4], a1 = x[1] + x[5], a2 = x[2] + x[6], a3 = x[3] + x[7];
+            const int b0 = x[0] - x[4], b1 = x[1] - x[5], b2 = x[2] - x[6], b3 = x[3] - x[7];
+            const int c0 = a0 + a2, c1 = a1 + a3, d0 = a0 - a2, d1 = a1 - a3;
+            y[0] = c0 + c1;
+            y[4] = c0 - c1;
+            const int t2 = f2 * d1;
+            y[2] = d0 + t2;
+            y[6] = d0 - t2;
+            const int e0 = b0 + f2 * b2, e1 = b0 - f2 * b2;
+            const int h1 = f1 * b1 + f3 * b3, h3 = f3 * b1 + f1 * b3;
+            y[1] = e0 + h1;
+            y[5] = e0 - h1;
+            y[3] = e1 + h3;
+            y[7] = e1 - h3;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                int acc = 0;
+#pragma unroll
+                for (int m = 0; m < 8; ++m) acc += x[m] * a.f8[8 * m + k];
+                y[k] = acc;
+            }
+        }
+        int o[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int2 t = __ldg(&a.tab[k * M + i]);
+            int z = r8red(y[k], t.x, t.y, a.q);
+            if (a.canonical) z = canon(z, a.q);
+            o[brev_c<3>(k)] = z;
+        }
+        int4 w;
+        w.x = (o[0] & 0xFFFF) | (o[1] << 16);
+        w.y = (o[2] & 0xFFFF) | (o[3] << 16);
+        w.z = (o[4] & 0xFFFF) | (o[5] << 16);
+        w.w = (o[6] & 0xFFFF) | (o[7] << 16);
+        *reinterpret_cast<int4*>(out + poly * n + 8 * i) = w;
+    }
+}
+
+// Bit-reversal unit (src/kernels/bitreverse_kernels.cc:54-143):
+// out[bitrev(i)] = in[i].  P polynomials per CTA are staged in shared memory
+// with coalesced 16-byte loads, then written back in order, each thread
+// reading the bit-reversed source position from shared memory.
+__global__ void __launch_bounds__(256) k_bitrev(const KArgs a, int L, int P) {
+    extern __shared__ short sb[];
+    const int n = 1 << L;
+    const long long poly0 = (long long)blockIdx.x * P;
+    long long np = a.batch - poly0;
+    if (np > P) np = P;
+    const int count = (int)np << L;
+    const short* src = static_cast<const short*>(a.in) + poly0 * n;
+    short* dst = static_cast<short*>(a.out) + poly0 * n;
+    if (n >= 8) {
+        for (int j = threadIdx.x; j < count / 8; j += blockDim.x)
+            reinterpret_cast<int4*>(sb)[j] = __ldg(reinterpret_cast<const int4*>(src) + j);
+    } else {
+        for (int j = threadIdx.x; j < count; j += blockDim.x) sb[j] = src[j];
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < count; j += blockDim.x) {
+        const int lp = j >> L, jj = j & (n - 1);
+        dst[j] = sb[(lp << L) + (int)(__brev((unsigned)jj) >> (32 - L))];
+    }
+}
+
+// Full Barrett multiplication by a constant, fully reduced
+// (src/kernels/full_reduction_kernels.cc:33-195).
+__device__ __forceinline__ int fb16(int x, int fs, int wq, int q) {
+    const int mb = wrap16(rsz16(x * wq));     // m' = SRS_16(x w'), symmetric_zero (:204-212)
+    const int r = x * fs - q * mb;            // x F_s - m' q (:234-238)
+    const int lo = wrap16(r);                 // low 16 bits (:241)
+    const int sign = wrap16(r >> 16);         // floor(r / 2^16) (:228, :242)
+    return wrap16(lo - sign * q);             // (:261-272)
+}
+
+__global__ void __launch_bounds__(256) k_full_barrett(const KArgs a, long long total, int fs, int wq) {
+    const short* in = static_cast<const short*>(a.in);
+    short* out = static_cast<short*>(a.out);
+    const long long nvec = total >> 3;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < nvec; j += stride) {
+        const int4 w = __ldg(reinterpret_cast<const int4*>(in) + j);
+        int ww[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            const int lo = fb16((int)(short)(ww[h] & 0xFFFF), fs, wq, a.q);
+            const int hi = fb16(ww[h] >> 16, fs, wq, a.q);
+            ww[h] = (lo & 0xFFFF) | (hi << 16);
+        }
+        reinterpret_cast<int4*>(out)[j] = make_int4(ww[0], ww[1], ww[2], ww[3]);
+    }
+    for (long long j = (nvec << 3) + (long long)blockIdx.x * blockDim.x + threadIdx.x; j < total; j += stride)
+        out[j] = (short)fb16(in[j], fs, wq, a.q);
+}
+
+int grid_for(long long work, int threads) {
+    long long b = (work + threads - 1) / threads;
+    const long long cap = 152LL * 16;
+    if (b > cap) b = cap;
+    return b < 1 ? 1 : (int)b;
+}
+
+}  // namespace
+
+int bitrev_smem_bytes(int L) {
+    const int n = 1 << L;
+    const int P = n >= 8192 ? 1 : 8192 / n;
+    return P * n * 2;
+}
+
+cudaError_t launch_r8_stage(const KArgs& a, int L, cudaStream_t s) {
+    const long long work = a.batch << (L - 3);
+    k_r8_stage<<<grid_for(work, 256), 256, 0, s>>>(a, L);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bitrev(const KArgs& a, int L, cudaStream_t s) {
+    const int n = 1 << L;
+    const int P = n >= 8192 ? 1 : 8192 / n;
+    const long long blocks = (a.batch + P - 1) / P;
+    const int smem = P * n * 2;
+    k_bitrev<<<(unsigned)blocks, 256, smem, s>>>(a, L, P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_full_barrett(const KArgs& a, long long total, int fs, int wq, cudaStream_t s) {
+    k_full_barrett<<<grid_for((total + 7) / 8, 256), 256, 0, s>>>(a, total, fs, wq);
+    return cudaGetLastError();
+}
+
+const void* bitrev_kernel_ptr() { return reinterpret_cast<const void*>(&k_bitrev); }
+
+}  // namespace gbntt

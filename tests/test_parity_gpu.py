@@ -1,0 +1,238 @@
+"""GPU parity: every design, through the C ABI, bit-exact against the oracle
+(the reference's algorithm restated on the CPU) on the same seeded inputs."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+SEED = 20261203
+
+
+@pytest.fixture(scope="module")
+def gb():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import ntts_on_amd_ai_engines_aie1_gb300 as gb
+    from ntts_on_amd_ai_engines_aie1_gb300 import build
+    build.build()
+    return gb
+
+
+def root_for(q, n):
+    if q == 12289:
+        return pow(41, 4096 // n, q)
+    if q == 1073707009:
+        return pow(992735929, 2048 // n, q)
+    g = {7681: 17, 10753: 11, 998244353: 3, 469762049: 3, 167772161: 3, 754974721: 11}[q]
+    return pow(g, (q - 1) // n, q)
+
+
+def gpu_run(gb, kind, n, q, root, x, factor=0, flags=0, inplace=False):
+    plan = gb.Plan(kind, n, q, root, factor, flags)
+    t = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    if inplace:
+        plan(t, out=t)
+        out = t
+    else:
+        out = plan(t)
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def inputs(rng, batch, n, lo, hi, dtype):
+    return rng.integers(lo, hi, size=(batch, n)).astype(dtype)
+
+
+def check(gb, orc, kind, okind, n, q, root, x, factor=0, flags=0, oflags=None, **kw):
+    want = orc.Plan(okind, n, q, root, factor=factor, **(oflags or {}))(x)
+    got = gpu_run(gb, kind, n, q, root, x, factor, flags)
+    assert got.dtype == want.dtype
+    bad = np.argwhere(got != want)
+    assert bad.size == 0, f"{len(bad)} mismatches, first at {bad[0]}: gpu {got[tuple(bad[0])]} oracle {want[tuple(bad[0])]}"
+    return want
+
+
+N16 = [2, 4, 8, 16, 32, 64, 128, 256, 512, 1024, 2048, 4096]
+
+
+@pytest.mark.parametrize("n", N16)
+def test_r2_i16_forward(gb, orc, n):
+    rng = np.random.default_rng(SEED + n)
+    q = 12289
+    for lo, hi in ((0, q), (-32768, 32768)):
+        x = inputs(rng, 37, n, lo, hi, np.int16)
+        check(gb, orc, gb.Kind.R2_I16_FWD, orc.R2_I16_FWD, n, q, root_for(q, n), x)
+
+
+@pytest.mark.parametrize("n", N16)
+def test_r2_i16_inverse(gb, orc, n):
+    rng = np.random.default_rng(SEED + 100 + n)
+    q = 12289
+    for lo, hi in ((-q, q), (-32768, 32768)):
+        x = inputs(rng, 29, n, lo, hi, np.int16)
+        check(gb, orc, gb.Kind.R2_I16_INV, orc.R2_I16_INV, n, q, root_for(q, n), x)
+
+
+@pytest.mark.parametrize("n,q", [(4, 12289), (16, 12289), (64, 12289), (256, 12289), (1024, 12289),
+                                 (4096, 12289), (256, 7681), (64, 10753), (256, 10753)])
+def test_r4_forward(gb, orc, n, q):
+    rng = np.random.default_rng(SEED + 200 + n + q)
+    for lo, hi in ((0, q), (-32768, 32768)):
+        x = inputs(rng, 41, n, lo, hi, np.int16)
+        check(gb, orc, gb.Kind.R4_I16_FWD, orc.R4_I16_FWD, n, q, root_for(q, n), x)
+
+
+@pytest.mark.parametrize("n", [4, 16, 256, 1024, 4096])
+def test_r4_inverse(gb, orc, n):
+    rng = np.random.default_rng(SEED + 300 + n)
+    q = 12289
+    x = inputs(rng, 9, n, -q, q, np.int16)
+    check(gb, orc, gb.Kind.R4_I16_INV, orc.R4_I16_INV, n, q, root_for(q, n), x)
+
+
+@pytest.mark.parametrize("n", [16, 64, 512, 1024, 4096])
+def test_r8_stage_reference_multipliers(gb, orc, n):
+    """The reference's one radix-8 stage with its float K=31 multipliers:
+    bit-exact, including the outputs those multipliers get wrong."""
+    rng = np.random.default_rng(SEED + 400 + n)
+    q = 12289
+    for lo, hi in ((0, q), (-32768, 32768)):
+        x = inputs(rng, 23, n, lo, hi, np.int16)
+        check(gb, orc, gb.Kind.R8_I16_STAGE, orc.R8_I16_STAGE, n, q, root_for(q, n), x)
+
+
+@pytest.mark.parametrize("n", [8, 16, 32, 64, 128, 256, 512, 1024, 2048, 4096])
+def test_r8_chained(gb, orc, n):
+    rng = np.random.default_rng(SEED + 500 + n)
+    q = 12289
+    x = inputs(rng, 19, n, -32768, 32768, np.int16)
+    check(gb, orc, gb.Kind.R8_I16_FWD, orc.R8_I16_FWD, n, q, root_for(q, n), x, oflags={"r8_exact": True})
+    check(gb, orc, gb.Kind.R8_I16_FWD, orc.R8_I16_FWD, n, q, root_for(q, n), x, flags=gb.FLAG_R8_FLOAT)
+
+
+Q32 = [998244353, 469762049, 167772161, 754974721, 1073707009]
+
+
+@pytest.mark.parametrize("n", [2, 4, 16, 64, 256, 1024, 2048, 4096, 8192, 16384, 32768])
+@pytest.mark.parametrize("q", Q32)
+def test_r2_i32(gb, orc, n, q):
+    if q == 1073707009 and n > 2048:
+        pytest.skip("root order 2048")
+    rng = np.random.default_rng(SEED + 600 + n + q % 1000)
+    batch = 7 if n >= 8192 else 33
+    root = root_for(q, n)
+    x = inputs(rng, batch, n, 0, q, np.int32)
+    y = check(gb, orc, gb.Kind.R2_I32_FWD, orc.R2_I32_FWD, n, q, root, x)
+    check(gb, orc, gb.Kind.R2_I32_INV, orc.R2_I32_INV, n, q, root, y)
+    xf = inputs(rng, batch, n, -(1 << 31), 1 << 31, np.int32)
+    check(gb, orc, gb.Kind.R2_I32_FWD, orc.R2_I32_FWD, n, q, root, xf)
+    check(gb, orc, gb.Kind.R2_I32_INV, orc.R2_I32_INV, n, q, root, xf)
+
+
+@pytest.mark.parametrize("n", [2, 8, 256, 512, 1024, 2048, 4096, 8192, 65536])
+def test_bitrev(gb, orc, n):
+    rng = np.random.default_rng(SEED + 700 + n)
+    x = inputs(rng, 5, n, -32768, 32768, np.int16)
+    got = gpu_run(gb, gb.Kind.BITREV_I16, n, 0, 0, x)
+    want = orc.Plan(orc.BITREV_I16, n)(x)
+    assert np.array_equal(got, want)
+    got2 = gpu_run(gb, gb.Kind.BITREV_I16, n, 0, 0, x, inplace=True)
+    assert np.array_equal(got2, want)
+
+
+@pytest.mark.parametrize("n,batch", [(4096, 3), (1024, 17), (7, 5)])
+def test_full_barrett(gb, orc, n, batch):
+    rng = np.random.default_rng(SEED + 800 + n)
+    q = 12289
+    F = pow(4096, -1, q)
+    x = inputs(rng, batch, n, -32768, 32768, np.int16)
+    got = gpu_run(gb, gb.Kind.FULL_BARRETT_I16, n, q, 0, x, factor=F)
+    want = orc.Plan(orc.FULL_BARRETT_I16, n, q, 0, factor=F)(x)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("kind,okind,q,n,dt", [(0, 0, 12289, 1024, np.int16), (1, 1, 12289, 1024, np.int16),
+                                               (2, 2, 12289, 1024, np.int16), (4, 4, 998244353, 4096, np.int32),
+                                               (5, 5, 754974721, 4096, np.int32)])
+def test_canonical_outputs(gb, orc, kind, okind, q, n, dt):
+    rng = np.random.default_rng(SEED + 900 + kind)
+    x = inputs(rng, 11, n, 0, q, dt)
+    want = orc.Plan(okind, n, q, root_for(q, n))(x).astype(np.int64) % q
+    got = gpu_run(gb, kind, n, q, root_for(q, n), x, flags=gb.FLAG_CANONICAL)
+    assert np.array_equal(got.astype(np.int64), want)
+
+
+@pytest.mark.parametrize("kind,okind,q,n,dt", [(0, 0, 12289, 4096, np.int16), (5, 5, 998244353, 4096, np.int32),
+                                               (8, 8, 12289, 2048, np.int16)])
+def test_in_place(gb, orc, kind, okind, q, n, dt):
+    rng = np.random.default_rng(SEED + 950 + kind)
+    x = inputs(rng, 6, n, 0, q, dt)
+    want = orc.Plan(okind, n, q, root_for(q, n), r8_exact=True)(x)
+    got = gpu_run(gb, kind, n, q, root_for(q, n), x, inplace=True)
+    assert np.array_equal(got, want)
+
+
+def test_config1_roundtrip(gb, orc):
+    """n = 1024, q = 12289: forward then inverse; bit-exact and x * n mod q."""
+    q, n = 12289, 1024
+    root = root_for(q, n)
+    x = np.random.default_rng(SEED).integers(0, q, n).astype(np.int16)
+    y = check(gb, orc, gb.Kind.R2_I16_FWD, orc.R2_I16_FWD, n, q, root, x[None])
+    z = check(gb, orc, gb.Kind.R2_I16_INV, orc.R2_I16_INV, n, q, root, y)
+    assert np.array_equal(z[0].astype(np.int64) % q, x.astype(np.int64) * n % q)
+    fb = gpu_run(gb, gb.Kind.FULL_BARRETT_I16, n, q, 0, z, factor=pow(n, -1, q))
+    assert np.array_equal(fb[0].astype(np.int64) % q, x.astype(np.int64))
+
+
+@pytest.mark.parametrize("q", [998244353, 469762049, 167772161, 754974721])
+def test_config2_dft(gb, orc, q):
+    """n = 256 against the O(n^2) DFT, n = 4096 round trip."""
+    rng = np.random.default_rng(SEED + q % 997)
+    x = rng.integers(0, q, 256)
+    y = gpu_run(gb, gb.Kind.R2_I32_FWD, 256, q, root_for(q, 256), x.astype(np.int32)[None], flags=gb.FLAG_CANONICAL)
+    X = orc.dft(x, q, root_for(q, 256))
+    assert np.array_equal(y[0].astype(np.int64), X[orc.bitrev_perm(256)])
+    x = rng.integers(0, q, 4096).astype(np.int32)[None]
+    y = gpu_run(gb, gb.Kind.R2_I32_FWD, 4096, q, root_for(q, 4096), x)
+    z = gpu_run(gb, gb.Kind.R2_I32_INV, 4096, q, root_for(q, 4096), y)
+    assert np.array_equal(z.astype(np.int64) % q, x.astype(np.int64) * 4096 % q)
+
+
+def test_graph_mirror_and_configs(gb, orc):
+    """dut_for_config selects the design of src/project.cpp:139-157."""
+    rng = np.random.default_rng(SEED + 1)
+    for cfg in range(8):
+        g = gb.dut_for_config(cfg).init()
+        p = g.plan
+        n = p.n
+        dt = np.int32 if p.elem_bytes == 4 else np.int16
+        x = rng.integers(0, min(p.q, 30000) if p.q else 30000, (3, n)).astype(dt)
+        out = g.run(3, torch.from_numpy(x).cuda())
+        torch.cuda.synchronize()
+        ok = orc.Plan(int(p.kind), n, p.q, p.root, factor=p.factor)(x)
+        assert np.array_equal(out.cpu().numpy(), ok), cfg
+        g.end()
+
+
+def test_batch_zero_and_launch_counter(gb):
+    plan = gb.Plan(gb.Kind.R2_I16_FWD, 1024, 12289, root_for(12289, 1024))
+    x = torch.zeros(4, 1024, dtype=torch.int16, device="cuda")
+    c0 = gb.launch_count()
+    plan.execute(x, x, 0)
+    assert gb.launch_count() == c0
+    plan(x)
+    assert gb.launch_count() == c0 + 1
+
+
+def test_execute_host(gb, orc):
+    q, n = 12289, 1024
+    x = np.random.default_rng(3).integers(-32768, 32768, (64, n)).astype(np.int16)
+    out = np.empty_like(x)
+    plan = gb.Plan(gb.Kind.R4_I16_FWD, n, q, root_for(q, n))
+    plan.execute_host(x, out)
+    assert np.array_equal(out, orc.Plan(orc.R4_I16_FWD, n, q, root_for(q, n))(x))
+    st = gb.Plan(gb.Kind.R8_I16_STAGE, n, q, root_for(q, n))
+    st.execute_host(x, out)
+    assert np.array_equal(out, orc.Plan(orc.R8_I16_STAGE, n, q, root_for(q, n))(x))
