@@ -281,20 +281,30 @@ def run_ours(args):
                    "batched_speedup": (polys / (ms / 1e3)) / (polys / (pm / 1e3))}
 
     # end to end through the C ABI on pinned host buffers
-    h_in = [torch.from_numpy(x).pin_memory() for x in inputs]
-    h_out = [torch.empty_like(x).pin_memory() for x in h_in]
-    e2e_steps = max(3, min(args.steps, 100))
-    for _ in range(min(args.warmup, 5)):
-        for i in range(len(SEGMENTS)):
-            plans[i].execute_host(h_in[i], h_out[i], SEGMENTS[i][2], stream)
-    e2e_t = []
-    for _ in range(e2e_steps):
-        t0 = time.perf_counter()
-        for i in range(len(SEGMENTS)):
-            plans[i].execute_host(h_in[i], h_out[i], SEGMENTS[i][2], stream)
-        e2e_t.append(time.perf_counter() - t0)
-    e2e_ms = 1e3 * sum(e2e_t) / len(e2e_t)
-    assert np.array_equal(h_out[2][:64].numpy(), oracle.Plan(oracle.R4_I16_FWD, 1024, 12289, 11580)(inputs[2][:64]))
+    e2e = None
+    if args.skip_e2e:
+        h_in = None
+    else:
+        e2e = True
+        h_in = [torch.from_numpy(x).pin_memory() for x in inputs]
+    if e2e:
+        h_out = [torch.empty_like(x).pin_memory() for x in h_in]
+        e2e_steps = max(3, min(args.steps, 100))
+        for _ in range(min(args.warmup, 5)):
+            for i in range(len(SEGMENTS)):
+                plans[i].execute_host(h_in[i], h_out[i], SEGMENTS[i][2], stream)
+        e2e_t = []
+        for _ in range(e2e_steps):
+            t0 = time.perf_counter()
+            for i in range(len(SEGMENTS)):
+                plans[i].execute_host(h_in[i], h_out[i], SEGMENTS[i][2], stream)
+            e2e_t.append(time.perf_counter() - t0)
+        e2e_ms = 1e3 * sum(e2e_t) / len(e2e_t)
+        assert np.array_equal(h_out[2][:64].numpy(),
+                              oracle.Plan(oracle.R4_I16_FWD, 1024, 12289, 11580)(inputs[2][:64]))
+        e2e = {"value": polys / (e2e_ms / 1e3), "unit": "NTT/s", "h2d_bytes_per_step": algo_bytes // 2,
+               "d2h_bytes_per_step": algo_bytes // 2, "ms_per_step": e2e_ms, "steps": e2e_steps,
+               "api": "gbntt_execute_host per segment (pinned host buffers)"}
 
     if rank != 0:
         if dist:
@@ -321,9 +331,7 @@ def run_ours(args):
                      "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": dom_avg,
                      "traffic": (traffic or {}).get("bytes_per_launch")},
         "cpu_baseline": cpu,
-        "e2e": {"value": polys / (e2e_ms / 1e3), "unit": "NTT/s", "h2d_bytes_per_step": algo_bytes // 2,
-                "d2h_bytes_per_step": algo_bytes // 2, "ms_per_step": e2e_ms, "steps": e2e_steps,
-                "api": "gbntt_execute_host per segment (pinned host buffers)"},
+        "e2e": e2e,
         "per_ntt_launch": per_ntt,
         "gpu_launches": launches,
         "clocks": sampler.summary(t_wall0, t_wall1),
@@ -331,6 +339,42 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+PROFILE_CASES = {
+    # name: (kind, n, q, root, polys) -- a few hundred MiB, inputs larger than L2
+    "r4_1024": (2, 1024, 12289, 11580, 65536),
+    "r2f16_1024": (0, 1024, 12289, 11580, 65536),
+    "r2i16_1024": (1, 1024, 12289, 11580, 65536),
+    "r2f32_4096": (4, 4096, 998244353, 63912897, 16384),
+    "r2g32_4096": (5, 4096, 998244353, 63912897, 16384),
+    "r8_4096": (8, 4096, 12289, 41, 16384),
+}
+
+
+def run_profile_case(name, launches=3):
+    """One design on one large batch, `launches` times (for ncu captures)."""
+    import torch
+
+    import ntts_on_amd_ai_engines_aie1_gb300 as gb
+    kind, n, q, root, polys = PROFILE_CASES[name]
+    plan = gb.Plan(kind, n, q, root)
+    dt = torch.int32 if plan.elem_bytes == 4 else torch.int16
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    x = torch.randint(0, q, (polys, n), dtype=torch.int64, device="cuda", generator=g).to(dt)
+    y = torch.empty_like(x)
+    for _ in range(launches):
+        plan(x, out=y)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    plan(x, out=y)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    nbytes = 2 * x.numel() * x.element_size()
+    print(json.dumps({"case": name, "kind": kind, "n": n, "q": q, "polys": polys, "ms": ms,
+                      "algorithmic_GBps": nbytes / (ms / 1e3) / 1e9}))
 
 
 def main():
@@ -342,7 +386,13 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=6.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-per-ntt", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--profile", choices=sorted(PROFILE_CASES), default=None,
+                    help="run one design on a large batch (for ncu captures) instead of the benchmark")
     args = ap.parse_args()
+    if args.profile:
+        run_profile_case(args.profile)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

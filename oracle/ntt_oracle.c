@@ -295,8 +295,11 @@ orc_plan* orc_plan_create(int kind, int n, int64_t q, int64_t root, int64_t fact
     orc_plan* p = NULL;
     int L = ilog2_exact(n);
     int is32 = (kind == ORC_R2_I32_FWD || kind == ORC_R2_I32_INV);
-    if (L < 1 || L > 24) { e = 1; goto fail; }
     if (kind < 0 || kind > ORC_R4_I16_INV) { e = 6; goto fail; }
+    if (kind == ORC_FULL_BARRETT_I16) {
+        if (n < 1) { e = 1; goto fail; }   /* elementwise: any length */
+        if (L < 0) L = 0;
+    } else if (L < 1 || L > 24) { e = 1; goto fail; }
     if (kind != ORC_BITREV_I16) {
         if (q < 3 || !(q & 1)) { e = 2; goto fail; }
         if (is32 ? (q >= 1431655765LL) : (q >= 21846)) { e = 4; goto fail; }
