@@ -185,6 +185,7 @@ def run_ours(args):
     import torch
 
     import ntts_on_amd_ai_engines_aie1_gb300 as gb
+    from oracle import oracle
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -199,72 +200,66 @@ def run_ours(args):
     plans = [gb.Plan(gb.Kind.R4_I16_FWD, n, q, root_of(q, n, g)) for (q, n, _, g) in SEGMENTS]
     d_in = [torch.from_numpy(x).to(dev) for x in inputs]
     d_out = [torch.empty_like(x) for x in d_in]
+    batch = gb.Batch([(plans[i], d_in[i], d_out[i]) for i in range(len(SEGMENTS))])
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
     polys = sum(cnt for _, _, cnt, _ in SEGMENTS)
     algo_bytes = sum(2 * n * 2 * cnt for _, n, cnt, _ in SEGMENTS)
-    dom = 2  # dominant kernel: the n = 1024, q = 12289 segment
-    dom_bytes = 2 * SEGMENTS[dom][1] * 2 * SEGMENTS[dom][2]
 
-    # correctness gate on the timed data (bit-exact vs the oracle on a sample)
-    from oracle import oracle
-    for i, (q, n, _, g) in enumerate(SEGMENTS):
-        plans[i](d_in[i], out=d_out[i])
+    # correctness gate on the timed data: every polynomial, bit-exact vs the oracle
+    batch.execute(stream)
     torch.cuda.synchronize()
+    batch.status()
     for i, (q, n, _, g) in enumerate(SEGMENTS):
-        want = oracle.Plan(oracle.R4_I16_FWD, n, q, root_of(q, n, g))(inputs[i][:64])
-        assert np.array_equal(d_out[i][:64].cpu().numpy(), want), "GPU output differs from the oracle"
+        want = oracle.Plan(oracle.R4_I16_FWD, n, q, root_of(q, n, g))(inputs[i], threads=os.cpu_count() or 1)
+        assert np.array_equal(d_out[i].cpu().numpy(), want), "GPU output differs from the oracle"
 
-    def step():
-        for i in range(len(SEGMENTS)):
-            plans[i].execute(d_in[i], d_out[i], SEGMENTS[i][2], stream)
+    def timed(run, steps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for a, b in evs:
+            flush.zero_()
+            a.record(stream)
+            run()
+            b.record(stream)
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in evs]
 
     for _ in range(args.warmup):
         flush.zero_()
-        step()
+        batch.graph_launch(stream)
     torch.cuda.synchronize()
     sampler = ClockSampler(local)
     time.sleep(0.3)
-    # keep the GPU loaded briefly so the sampler sees clocks under load
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
-           torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     launches0 = gb.launch_count()
     t_wall0 = time.time()
-    for i in range(args.steps):
-        flush.zero_()
-        e0, e1, k0, k1 = ev[i]
-        e0.record(stream)
-        plans[0].execute(d_in[0], d_out[0], SEGMENTS[0][2], stream)
-        plans[1].execute(d_in[1], d_out[1], SEGMENTS[1][2], stream)
-        k0.record(stream)
-        plans[2].execute(d_in[2], d_out[2], SEGMENTS[2][2], stream)
-        k1.record(stream)
-        e1.record(stream)
-    torch.cuda.synchronize()
+    step_ms = timed(lambda: batch.graph_launch(stream), args.steps)
     t_wall1 = time.time()
     launches = gb.launch_count() - launches0
     if dist:
         dist.barrier()
     sampler.stop()
-    step_ms = [a.elapsed_time(b) for a, b, _, _ in ev]
-    dom_ms = [c.elapsed_time(d) for _, _, c, d in ev]
+    batch.status()
     ms = sum(step_ms) / len(step_ms)
     if dist:
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = world * polys / (ms / 1e3)
-    dom_avg = sum(dom_ms) / len(dom_ms)
     peak, peak_src = load_peaks()
-    achieved = dom_bytes / (dom_avg / 1e3) / 1e9
+    achieved = algo_bytes / (ms / 1e3) / 1e9
     traffic = load_traffic()
 
-    # plain per-NTT launches of the same batch (the baseline the metric names)
-    per_ntt = None
+    extra = {}
     if rank == 0 and not args.skip_per_ntt:
+        # the same batch as one launch per segment (plan path) ...
+        pp = timed(lambda: [plans[i].execute(d_in[i], d_out[i], SEGMENTS[i][2], stream)
+                            for i in range(len(SEGMENTS))], min(args.steps, 200))
+        pms = sum(pp) / len(pp)
+        extra["per_segment_launches"] = {"value": polys / (pms / 1e3), "unit": "NTT/s", "launches_per_step": 3}
+        # ... and as plain per-NTT launches (one launch per polynomial)
         flush.zero_()
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -277,34 +272,29 @@ def run_ours(args):
         b.record(stream)
         torch.cuda.synchronize()
         pm = a.elapsed_time(b)
-        per_ntt = {"value": polys / (pm / 1e3), "unit": "NTT/s", "launches": polys,
-                   "batched_speedup": (polys / (ms / 1e3)) / (polys / (pm / 1e3))}
+        extra["per_ntt_launch"] = {"value": polys / (pm / 1e3), "unit": "NTT/s", "launches": polys,
+                                   "batched_speedup": (polys / (ms / 1e3)) / (polys / (pm / 1e3))}
 
-    # end to end through the C ABI on pinned host buffers
     e2e = None
-    if args.skip_e2e:
-        h_in = None
-    else:
-        e2e = True
+    if not args.skip_e2e:
+        # end to end through the C ABI: pinned host buffers, H2D + one launch + D2H per step
         h_in = [torch.from_numpy(x).pin_memory() for x in inputs]
-    if e2e:
         h_out = [torch.empty_like(x).pin_memory() for x in h_in]
         e2e_steps = max(3, min(args.steps, 100))
         for _ in range(min(args.warmup, 5)):
-            for i in range(len(SEGMENTS)):
-                plans[i].execute_host(h_in[i], h_out[i], SEGMENTS[i][2], stream)
+            batch.execute_host(h_in, h_out, stream)
         e2e_t = []
         for _ in range(e2e_steps):
             t0 = time.perf_counter()
-            for i in range(len(SEGMENTS)):
-                plans[i].execute_host(h_in[i], h_out[i], SEGMENTS[i][2], stream)
+            batch.execute_host(h_in, h_out, stream)
             e2e_t.append(time.perf_counter() - t0)
         e2e_ms = 1e3 * sum(e2e_t) / len(e2e_t)
-        assert np.array_equal(h_out[2][:64].numpy(),
-                              oracle.Plan(oracle.R4_I16_FWD, 1024, 12289, 11580)(inputs[2][:64]))
+        for i, (q, n, _, g) in enumerate(SEGMENTS):
+            want = oracle.Plan(oracle.R4_I16_FWD, n, q, root_of(q, n, g))(inputs[i][:128])
+            assert np.array_equal(h_out[i][:128].numpy(), want)
         e2e = {"value": polys / (e2e_ms / 1e3), "unit": "NTT/s", "h2d_bytes_per_step": algo_bytes // 2,
                "d2h_bytes_per_step": algo_bytes // 2, "ms_per_step": e2e_ms, "steps": e2e_steps,
-               "api": "gbntt_execute_host per segment (pinned host buffers)"}
+               "api": "gbntt_batch_execute_host (pinned host buffers, wall clock)"}
 
     if rank != 0:
         if dist:
@@ -321,21 +311,21 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "NTT/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int16", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "polys_per_step": polys, "coefficients_per_step": polys and
-                   sum(n * cnt for _, n, cnt, _ in SEGMENTS), "algorithmic_bytes_per_step": algo_bytes,
-                   "hbm_gbs_whole_step": algo_bytes / (ms / 1e3) / 1e9,
+        "config": {"workload": WORKLOAD, "polys_per_step": polys,
+                   "coefficients_per_step": sum(n * cnt for _, n, cnt, _ in SEGMENTS),
+                   "algorithmic_bytes_per_step": algo_bytes, "launch": "one persistent kernel, CUDA graph replay",
                    "l2": "flushed before every step (256 MiB write, untimed)", "parallelism": f"replicas{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src,
-                     "kernel": "k_ntt radix-4 n=1024 q=12289 (8192 polys per launch)",
-                     "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": dom_avg,
+                     "kernel": "k_batch<int16> persistent radix-4 (all 16384 polys per launch)",
+                     "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_ms": ms,
                      "traffic": (traffic or {}).get("bytes_per_launch")},
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "per_ntt_launch": per_ntt,
         "gpu_launches": launches,
         "clocks": sampler.summary(t_wall0, t_wall1),
     }
+    line.update(extra)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -349,7 +339,36 @@ PROFILE_CASES = {
     "r2f32_4096": (4, 4096, 998244353, 63912897, 16384),
     "r2g32_4096": (5, 4096, 998244353, 63912897, 16384),
     "r8_4096": (8, 4096, 12289, 41, 16384),
+    "batch_r4": None,   # the benchmark batch, 4x larger, persistent kernel
 }
+
+
+def run_profile_batch(scale=4, launches=3):
+    """The benchmark's batch with every segment `scale` times larger (inputs
+    larger than L2), executed `launches` times as one persistent launch."""
+    import torch
+
+    import ntts_on_amd_ai_engines_aie1_gb300 as gb
+    rng = np.random.default_rng(SEED)
+    plans, xs, ys = [], [], []
+    for q, n, cnt, g in SEGMENTS:
+        plans.append(gb.Plan(gb.Kind.R4_I16_FWD, n, q, root_of(q, n, g)))
+        xs.append(torch.from_numpy(rng.integers(0, q, (cnt * scale, n)).astype(np.int16)).cuda())
+        ys.append(torch.empty_like(xs[-1]))
+    batch = gb.Batch(list(zip(plans, xs, ys)))
+    for _ in range(launches):
+        batch.execute()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    batch.execute()
+    b.record()
+    torch.cuda.synchronize()
+    batch.status()
+    ms = a.elapsed_time(b)
+    nbytes = sum(2 * x.numel() * 2 for x in xs)
+    print(json.dumps({"case": f"batch_x{scale}", "polys": sum(x.shape[0] for x in xs), "ms": ms,
+                      "algorithmic_GBps": nbytes / (ms / 1e3) / 1e9}))
 
 
 def run_profile_case(name, launches=3):
@@ -357,6 +376,8 @@ def run_profile_case(name, launches=3):
     import torch
 
     import ntts_on_amd_ai_engines_aie1_gb300 as gb
+    if name == "batch_r4":
+        return run_profile_batch(4, launches)
     kind, n, q, root, polys = PROFILE_CASES[name]
     plan = gb.Plan(kind, n, q, root)
     dt = torch.int32 if plan.elem_bytes == 4 else torch.int16

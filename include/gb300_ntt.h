@@ -122,6 +122,47 @@ int gbntt_plan_query(const gbntt_plan* plan, int what, int64_t* value);
 int gbntt_host_tables(int kind, uint32_t n, int64_t q, int64_t root, int64_t factor,
                       uint32_t flags, int which, int64_t* dst, int64_t cap, int64_t* len);
 
+/* ---- batches: many polynomials of several designs in one persistent launch ----
+ *
+ * A batch is a fixed list of segments (plan, device input, device output,
+ * number of polynomials).  gbntt_batch_execute transforms all of them with one
+ * persistent kernel launch per storage type (int16 designs, int32 designs):
+ * tiles of polynomials are handed out dynamically, largest n first, and move
+ * between HBM and shared memory as bulk (TMA) copies, double-buffered.
+ * Segments the persistent kernel does not cover (bit-reversal, full Barrett,
+ * the radix-8 single stage, the radix-4 inverse, in-place segments, n outside
+ * its range) run as their plans' own launches after it, on the same stream.
+ * The batch owns a few words of device scratch (tile counter), so launches of
+ * one batch must not overlap; different batches may run concurrently. */
+typedef struct gbntt_segment {
+    const gbntt_plan* plan;
+    const void* d_in;
+    void* d_out;
+    uint64_t count;
+} gbntt_segment;
+
+typedef struct gbntt_batch gbntt_batch;
+
+int gbntt_batch_create(gbntt_batch** batch, const gbntt_segment* segs, uint32_t nsegs, uint32_t flags);
+int gbntt_batch_execute(gbntt_batch* batch, void* stream);
+/* The same launches captured once in a CUDA graph and replayed. */
+int gbntt_batch_graph_launch(gbntt_batch* batch, void* stream);
+/* Host buffers: copies h_in[i] into segment i's device input, runs the batch
+ * (graph replay), copies every segment's device output to h_out[i] and waits
+ * for the stream.  Pinned host buffers give full copy bandwidth. */
+int gbntt_batch_execute_host(gbntt_batch* batch, const void* const* h_in, void* const* h_out, void* stream);
+/* Rebinds a segment's buffers (no launch of the batch may be in flight). */
+int gbntt_batch_set_io(gbntt_batch* batch, uint32_t seg, const void* d_in, void* d_out);
+/* Synchronous: GBNTT_ERR_TIMEOUT if a tile load of an earlier launch ran out
+ * of its bounded wait (the error is cleared by the call). */
+int gbntt_batch_status(gbntt_batch* batch);
+#define GBNTT_BQ_LAUNCHES 0   /* kernel launches per execute            */
+#define GBNTT_BQ_TILES    1   /* tiles of the persistent launches        */
+#define GBNTT_BQ_GRID     2   /* CTAs of the largest persistent launch   */
+#define GBNTT_BQ_SMEM     3   /* dynamic shared memory per CTA (bytes)   */
+int gbntt_batch_query(const gbntt_batch* batch, int what, int64_t* value);
+int gbntt_batch_destroy(gbntt_batch* batch);
+
 /* Total number of kernels this library has launched in this process. */
 uint64_t gbntt_launch_count(void);
 

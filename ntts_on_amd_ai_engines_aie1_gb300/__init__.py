@@ -54,6 +54,12 @@ class NTTError(RuntimeError):
         self.code = code
 
 
+class Segment(ctypes.Structure):
+    """gbntt_segment: plan, device input, device output, polynomial count."""
+    _fields_ = [("plan", ctypes.c_void_p), ("d_in", ctypes.c_void_p), ("d_out", ctypes.c_void_p),
+                ("count", ctypes.c_uint64)]
+
+
 _lib = None
 
 
@@ -73,6 +79,14 @@ def lib():
         L.gbntt_plan_query.argtypes = [vp, i32, ctypes.POINTER(i64)]
         L.gbntt_host_tables.argtypes = [i32, u32, i64, i64, i64, u32, i32, ctypes.POINTER(i64), i64,
                                         ctypes.POINTER(i64)]
+        L.gbntt_batch_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(Segment), u32, u32]
+        L.gbntt_batch_execute.argtypes = [vp, vp]
+        L.gbntt_batch_graph_launch.argtypes = [vp, vp]
+        L.gbntt_batch_set_io.argtypes = [vp, u32, vp, vp]
+        L.gbntt_batch_execute_host.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), vp]
+        L.gbntt_batch_status.argtypes = [vp]
+        L.gbntt_batch_query.argtypes = [vp, i32, ctypes.POINTER(i64)]
+        L.gbntt_batch_destroy.argtypes = [vp]
         L.gbntt_launch_count.restype = u64
         L.gbntt_last_error.restype = ctypes.c_char_p
         L.gbntt_status_string.restype = ctypes.c_char_p
@@ -172,6 +186,72 @@ class Plan:
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
             lib().gbntt_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many polynomials of several designs in one persistent launch.
+
+    segments: list of (plan, input tensor, output tensor); the tensors' first
+    dimension (or numel / n) gives the polynomial count.  The batch keeps
+    references to plans and tensors so they outlive it."""
+
+    def __init__(self, segments, flags=0):
+        self._keep = list(segments)
+        arr = (Segment * len(segments))()
+        for i, (plan, x, y) in enumerate(segments):
+            arr[i].plan = plan.handle
+            arr[i].d_in = _ptr(x)
+            arr[i].d_out = _ptr(y)
+            arr[i].count = (x.numel() // plan.n) if hasattr(x, "numel") else 0
+        h = ctypes.c_void_p()
+        _check(lib().gbntt_batch_create(ctypes.byref(h), arr, len(segments), flags))
+        self._h = h
+
+    def execute(self, stream=None):
+        _check(lib().gbntt_batch_execute(self._h, _stream_ptr(stream)))
+
+    def graph_launch(self, stream=None):
+        _check(lib().gbntt_batch_graph_launch(self._h, _stream_ptr(stream)))
+
+    def execute_host(self, h_in, h_out, stream=None):
+        """Host arrays (one per segment, pinned for full bandwidth); synchronous."""
+        def p(a):
+            return a.ctypes.data if hasattr(a, "ctypes") else a.data_ptr()
+        ins = (ctypes.c_void_p * len(h_in))(*[p(a) for a in h_in])
+        outs = (ctypes.c_void_p * len(h_out))(*[p(a) for a in h_out])
+        _check(lib().gbntt_batch_execute_host(self._h, ins, outs, _stream_ptr(stream)))
+
+    def set_io(self, seg, x, y):
+        plan = self._keep[seg][0]
+        self._keep[seg] = (plan, x, y)
+        _check(lib().gbntt_batch_set_io(self._h, seg, _ptr(x), _ptr(y)))
+
+    def status(self):
+        _check(lib().gbntt_batch_status(self._h))
+
+    def query(self, what):
+        v = ctypes.c_int64(0)
+        _check(lib().gbntt_batch_query(self._h, what, ctypes.byref(v)))
+        return v.value
+
+    @property
+    def launches(self):
+        return self.query(0)
+
+    @property
+    def tiles(self):
+        return self.query(1)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().gbntt_batch_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

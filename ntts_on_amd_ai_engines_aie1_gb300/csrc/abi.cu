@@ -8,6 +8,7 @@
 
 #include "../../include/gb300_ntt.h"
 #include "device.cuh"
+#include "plan_internal.h"
 #include "tables.h"
 
 namespace gbntt {
@@ -94,6 +95,19 @@ int launch(const gbntt_plan* p, const void* d_in, void* d_out, uint64_t batch, c
 }
 
 }  // namespace
+
+int gbntt_internal_fail(int code, const std::string& msg) { return fail(code, msg); }
+
+void gbntt_internal_count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+int gbntt_internal_plan_L(const gbntt_plan* p) { return p ? p->hp.L : 0; }
+
+void gbntt_internal_plan_args(const gbntt_plan* p, int* fam, int* L, int* elem_bytes, KArgs* a) {
+    *fam = p->br ? -1 : p->fam;
+    *L = p->hp.L;
+    *elem_bytes = p->hp.elem_bytes;
+    *a = p->base;
+}
 
 extern "C" {
 

@@ -1,0 +1,196 @@
+// persist.cuh -- the persistent batched transform kernel.
+//
+// One launch transforms every polynomial of a batch made of segments (design,
+// n, q, input, output, count).  Work is cut into tiles of P polynomials
+// (P = CTA threads / G, G = threads per polynomial) and handed out by a global
+// atomic counter, largest n first.  Each CTA double-buffers its tiles in
+// shared memory with the Tensor Memory Accelerator's bulk copies:
+//
+//   cp.async.bulk global->shared (mbarrier complete_tx) prefetches tile t+1
+//   while tile t is transformed; the results are written back into the same
+//   shared buffer and leave with cp.async.bulk shared->global.
+//
+// Inside a tile every polynomial is transformed by the window/exchange scheme
+// of device.cuh with 32 coefficients per thread: with that width, the padded
+// exchange layout (one spare word per 32) is free of bank conflicts for every
+// window, and the strided staging layout is conflict-free as well.
+#pragma once
+
+#include "device.cuh"
+
+namespace gbntt {
+
+// scratch words of a batch (device memory owned by the batch object)
+enum { CTR_NEXT = 0, CTR_DONE = 1, CTR_ERROR = 2, CTR_WORDS = 4 };
+enum { BERR_TIMEOUT = 1 };
+
+struct SegDev {
+    KArgs a;              // in, out, batch (= polynomial count), tables, constants
+    long long tile0;      // first tile of the segment in the global tile order
+    long long tiles;      // number of tiles
+    int variant;          // (family << 4) | L
+    int polys_per_tile;   // P
+    int n;
+    int elem_bytes;
+};
+
+struct BatchDev {
+    const SegDev* segs;
+    int nsegs;
+    long long total_tiles;
+    unsigned long long* ctr;   // CTR_WORDS scratch words, zero between launches
+};
+
+constexpr int BATCH_EL = 5;
+__host__ __device__ constexpr int batch_el(int L) { return L < BATCH_EL ? L : BATCH_EL; }
+__host__ __device__ constexpr int variant_id(int fam, int L) { return (fam << 4) | L; }
+
+// ---------------------------------------------------------------------------
+// PTX wrappers: mbarrier and bulk (TMA) copies
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// Bounded wait for the phase `parity` of the barrier.  Returns false when the
+// iteration limit ran out (the caller records an error and stops).
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+    const unsigned a = smem_addr(bar);
+    for (int it = 0; it < (1 << 22); ++it) {
+        unsigned ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void bulk_load(void* dst_smem, const void* src_gmem, unsigned bytes,
+                                          unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst_smem)),
+        "l"(src_gmem), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void bulk_store(void* dst_gmem, const void* src_smem, unsigned bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst_gmem),
+                 "r"(smem_addr(src_smem)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// wait until the shared-memory sources of all committed bulk stores have been read
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// wait until all committed bulk stores are complete
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// make generic-proxy shared-memory writes visible to the bulk-copy (async) proxy
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// ---------------------------------------------------------------------------
+// one tile: P polynomials staged contiguously in shared memory
+// ---------------------------------------------------------------------------
+
+template <int L, int EL, int LOA, int LOB>
+__device__ __forceinline__ void exchange(int (&v)[1 << EL], int* sp, int g) {
+    constexpr int E = 1 << EL, G = 1 << (L - EL);
+    group_sync<G>();
+#pragma unroll
+    for (int k = 0; k < E; ++k) sp[spad(posmap<LOA, EL>(g, k))] = v[k];
+    group_sync<G>();
+#pragma unroll
+    for (int k = 0; k < E; ++k) v[k] = sp[spad(posmap<LOB, EL>(g, k))];
+}
+
+template <int FAM, int L, int CTA>
+__device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KArgs& a, int npolys) {
+    constexpr int EL = batch_el(L);
+    constexpr int G = 1 << (L - EL), N = 1 << L, E = 1 << EL;
+    constexpr int SW = N + N / 32;
+    constexpr int NS = nsteps(FAM, L);
+    constexpr int LOS = L - EL;                          // staging layout: strided, conflict-free
+    constexpr int LO0 = window_lo(FAM, L, EL, 0);
+    constexpr int LOZ = window_lo(FAM, L, EL, NS - 1);
+    constexpr bool I32 = fam_i32(FAM);
+    static_assert(CTA % G == 0, "a polynomial must not straddle CTAs");
+    const int tid = threadIdx.x;
+    const int lp = tid / G, g = tid % G;
+    const bool active = lp < npolys;
+    int* sp = xbuf + lp * SW;
+    int v[E];
+    if (active) {
+        if constexpr (I32) {
+            const int* s = static_cast<const int*>(stage) + lp * N;
+#pragma unroll
+            for (int k = 0; k < E; ++k) v[k] = s[posmap<LOS, EL>(g, k)];
+        } else {
+            const short* s = static_cast<const short*>(stage) + lp * N;
+#pragma unroll
+            for (int k = 0; k < E; ++k) v[k] = s[posmap<LOS, EL>(g, k)];
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < E; ++k) v[k] = 0;
+    }
+    if constexpr (LO0 != LOS) exchange<L, EL, LOS, LO0>(v, sp, g);
+    run_steps<FAM, L, EL>(v, sp, g, a, std::make_integer_sequence<int, NS>{});
+    if (a.canonical) {
+#pragma unroll
+        for (int k = 0; k < E; ++k) v[k] = canon(v[k], a.q);
+    }
+    if (!active) return;
+    if constexpr (LOZ == 0 && (I32 ? E >= 4 : E >= 8)) {
+        // thread owns E consecutive coefficients: 16-byte stores
+        if constexpr (I32) {
+            int4* d = reinterpret_cast<int4*>(static_cast<int*>(stage) + lp * N + g * E);
+#pragma unroll
+            for (int j = 0; j < E / 4; ++j) d[j] = make_int4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+        } else {
+            int4* d = reinterpret_cast<int4*>(static_cast<short*>(stage) + lp * N + g * E);
+#pragma unroll
+            for (int j = 0; j < E / 8; ++j) {
+                int w[4];
+#pragma unroll
+                for (int h = 0; h < 4; ++h) w[h] = (v[8 * j + 2 * h] & 0xFFFF) | (v[8 * j + 2 * h + 1] << 16);
+                d[j] = make_int4(w[0], w[1], w[2], w[3]);
+            }
+        }
+    } else {
+        if constexpr (I32) {
+            int* d = static_cast<int*>(stage) + lp * N;
+#pragma unroll
+            for (int k = 0; k < E; ++k) d[posmap<LOZ, EL>(g, k)] = v[k];
+        } else {
+            short* d = static_cast<short*>(stage) + lp * N;
+#pragma unroll
+            for (int k = 0; k < E; ++k) d[posmap<LOZ, EL>(g, k)] = (short)v[k];
+        }
+    }
+}
+
+// shared-memory bytes the persistent kernel needs for the largest variant of a batch
+__host__ __device__ constexpr int batch_stage_bytes(int cta, int L, int elem) {
+    // P * N = cta * E coefficients per tile
+    return cta * (1 << batch_el(L)) * elem;
+}
+__host__ __device__ constexpr int batch_xbuf_bytes(int cta, int L) {
+    return batch_el(L) == L ? 0 : (cta >> (L - batch_el(L))) * ((1 << L) + (1 << L) / 32) * 4;
+}
+
+}  // namespace gbntt

@@ -1,0 +1,14 @@
+// plan_internal.h -- accessors shared by abi.cu and batch.cu (not part of the ABI).
+#pragma once
+
+#include <string>
+
+#include "device.cuh"
+
+struct gbntt_plan;
+
+int gbntt_internal_fail(int code, const std::string& msg);
+void gbntt_internal_count_launch();
+int gbntt_internal_plan_L(const gbntt_plan* p);
+// family (-1 when the design has no persistent-kernel variant), log2 n, element bytes, launch constants
+void gbntt_internal_plan_args(const gbntt_plan* p, int* fam, int* L, int* elem_bytes, gbntt::KArgs* a);

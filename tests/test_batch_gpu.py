@@ -1,0 +1,108 @@
+"""Persistent batched launches: mixed designs, moduli and lengths in one
+launch per storage type, bit-exact against the oracle."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+from test_parity_gpu import root_for  # noqa: E402
+
+SEED = 4242
+
+
+@pytest.fixture(scope="module")
+def gb():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import ntts_on_amd_ai_engines_aie1_gb300 as gb
+    from ntts_on_amd_ai_engines_aie1_gb300 import build
+    build.build()
+    return gb
+
+
+SEGS = [
+    # (kind, oracle kind, n, q, count, dtype, flags, oracle kwargs)
+    (2, 2, 256, 7681, 700, np.int16, 0, {}),
+    (2, 2, 256, 10753, 513, np.int16, 0, {}),
+    (2, 2, 1024, 12289, 999, np.int16, 0, {}),
+    (0, 0, 1024, 12289, 77, np.int16, 0, {}),
+    (1, 1, 512, 12289, 65, np.int16, 0, {}),
+    (0, 0, 4096, 12289, 9, np.int16, 0, {}),
+    (1, 1, 8, 12289, 300, np.int16, 0, {}),
+    (8, 8, 4096, 12289, 11, np.int16, 0, {"r8_exact": True}),
+    (8, 8, 256, 12289, 37, np.int16, 0, {"r8_exact": True}),
+    (2, 2, 16, 12289, 1000, np.int16, 1, {}),
+    (4, 4, 4096, 998244353, 13, np.int32, 0, {}),
+    (5, 5, 2048, 754974721, 21, np.int32, 0, {}),
+    (4, 4, 8192, 469762049, 3, np.int32, 0, {}),
+    (5, 5, 4, 167772161, 999, np.int32, 0, {}),
+    (6, 6, 1024, 0, 10, np.int16, 0, {}),          # bit-reversal: separate launch
+    (3, 3, 512, 12289, 12, np.int16, 0, {}),       # radix-8 stage: separate launch
+]
+
+
+def _make(gb, rng, spec):
+    kind, okind, n, q, count, dt, flags, okw = spec
+    root = root_for(q, n) if q else 0
+    plan = gb.Plan(kind, n, q, root, 0, flags)
+    hi = q if q else 30000
+    x = rng.integers(-hi if dt == np.int16 else 0, hi, (count, n)).astype(dt)
+    want = __import__("oracle.oracle", fromlist=["Plan"]).Plan(okind, n, q, root, **okw)(x)
+    if flags & 1:
+        want = (want.astype(np.int64) % q).astype(dt)
+    return plan, x, want
+
+
+def test_mixed_batch(gb):
+    rng = np.random.default_rng(SEED)
+    made = [_make(gb, rng, s) for s in SEGS]
+    xs = [torch.from_numpy(x).cuda() for _, x, _ in made]
+    ys = [torch.full_like(x, 12345) for x in xs]
+    b = gb.Batch([(p, x, y) for (p, _, _), x, y in zip(made, xs, ys)])
+    assert b.launches == 2 + 2          # int16 + int32 persistent launches, bitrev, r8 stage
+    for rep in range(3):                # the tile counter re-arms itself
+        for y in ys:
+            y.fill_(12345)
+        b.execute()
+        torch.cuda.synchronize()
+        b.status()
+        for i, ((_, _, want), y) in enumerate(zip(made, ys)):
+            got = y.cpu().numpy()
+            assert np.array_equal(got, want), f"segment {i} ({SEGS[i][:5]}), repetition {rep}"
+
+
+def test_graph_launch_and_rebind(gb):
+    rng = np.random.default_rng(SEED + 1)
+    made = [_make(gb, rng, s) for s in SEGS[:4]]
+    xs = [torch.from_numpy(x).cuda() for _, x, _ in made]
+    ys = [torch.zeros_like(x) for x in xs]
+    b = gb.Batch([(p, x, y) for (p, _, _), x, y in zip(made, xs, ys)])
+    assert b.launches == 1
+    s = torch.cuda.Stream()
+    for _ in range(4):
+        b.graph_launch(s)
+    s.synchronize()
+    for (_, _, want), y in zip(made, ys):
+        assert np.array_equal(y.cpu().numpy(), want)
+    # rebind segment 2 to new buffers; the graph picks the new descriptor up
+    x2 = torch.from_numpy(rng.integers(0, 12289, (999, 1024)).astype(np.int16)).cuda()
+    y2 = torch.zeros_like(x2)
+    b.set_io(2, x2, y2)
+    b.graph_launch(s)
+    s.synchronize()
+    from oracle import oracle
+    want2 = oracle.Plan(2, 1024, 12289, root_for(12289, 1024))(x2.cpu().numpy())
+    assert np.array_equal(y2.cpu().numpy(), want2)
+
+
+def test_batch_counts_launches(gb):
+    plan = gb.Plan(2, 1024, 12289, root_for(12289, 1024))
+    x = torch.zeros(4096, 1024, dtype=torch.int16, device="cuda")
+    y = torch.empty_like(x)
+    b = gb.Batch([(plan, x, y)])
+    c0 = gb.launch_count()
+    b.execute()
+    torch.cuda.synchronize()
+    assert gb.launch_count() == c0 + 1
+    assert b.tiles == 4096 // 8
