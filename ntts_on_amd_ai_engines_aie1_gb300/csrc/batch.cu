@@ -34,10 +34,11 @@ __global__ void __launch_bounds__(CTA, I32 ? 2 : 3) k_batch(const BatchDev b, in
     extern __shared__ __align__(128) unsigned char smem[];
     unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem);
     KArgs* ka = reinterpret_cast<KArgs*>(smem + 64);
-    unsigned char* stage[2] = {smem + SMEM_HEADER, smem + SMEM_HEADER + stage_bytes};
+    unsigned char* stage0 = smem + SMEM_HEADER;
     int* xbuf = reinterpret_cast<int*>(smem + SMEM_HEADER + 2 * stage_bytes);
     __shared__ long long sh_next;
     __shared__ int sh_pending[2];
+    __shared__ int sh_failed;
     const int tid = threadIdx.x;
     const long long total = b.total_tiles;
 
@@ -56,7 +57,7 @@ __global__ void __launch_bounds__(CTA, I32 ? 2 : 3) k_batch(const BatchDev b, in
         const unsigned bytes = (unsigned)(np * sd->n * sd->elem_bytes);
         const char* src = static_cast<const char*>(sd->a.in) + lt * P * sd->n * sd->elem_bytes;
         mbar_expect_tx(&bar[i], bytes);
-        bulk_load(stage[i], src, bytes, &bar[i]);
+        bulk_load(stage0 + i * stage_bytes, src, bytes, &bar[i]);
     };
 
     if (tid == 0) {
@@ -67,6 +68,7 @@ __global__ void __launch_bounds__(CTA, I32 ? 2 : 3) k_batch(const BatchDev b, in
         sh_next = t0;
         sh_pending[0] = 0;
         sh_pending[1] = 0;
+        sh_failed = 0;
         if (t0 < total) {
             issue(t0, 0);
             sh_pending[0] = 1;
@@ -74,10 +76,10 @@ __global__ void __launch_bounds__(CTA, I32 ? 2 : 3) k_batch(const BatchDev b, in
     }
     __syncthreads();
     long long t = sh_next;
-    unsigned phase[2] = {0u, 0u};
+    unsigned phases = 0u;    // bit i: parity of the next completion of bar[i]
     int buf = 0;
     int cur_seg = -1;
-    bool failed = false;
+    KC kc;
     while (t < total) {
         const int s = seg_of(t);
         const SegDev* sd = &b.segs[s];
@@ -91,32 +93,25 @@ __global__ void __launch_bounds__(CTA, I32 ? 2 : 3) k_batch(const BatchDev b, in
             }
         }
         if (s != cur_seg) {
-            // the previous tile finished with the old arguments (barrier at the loop end)
+            // every thread finished the previous tile (barrier at the loop end)
             const int* src = reinterpret_cast<const int*>(&sd->a);
             int* dst = reinterpret_cast<int*>(ka);
             for (int w = tid; w < (int)(sizeof(KArgs) / 4); w += CTA) dst[w] = src[w];
             cur_seg = s;
+            __syncthreads();
+            kc = make_kc(*ka);
         }
-        const bool ok = mbar_wait(&bar[buf], phase[buf]);
-        phase[buf] ^= 1u;
-        if (__syncthreads_or(!ok)) {
-            failed = true;
-            if (tid == 0) {
-                sh_pending[buf] = 0;
-                atomicMax(&b.ctr[CTR_ERROR], (unsigned long long)BERR_TIMEOUT);
-            }
-            break;
-        }
-        if (tid == 0) sh_pending[buf] = 0;
-        const long long tnext = sh_next;
+        if (!mbar_wait(&bar[buf], (phases >> buf) & 1u)) sh_failed = 1;
+        phases ^= 1u << buf;
         const long long lt = t - sd->tile0;
         const int P = sd->polys_per_tile;
         const int np = (int)min((long long)P, sd->a.batch - lt * P);
-        void* st = stage[buf];
-        switch (sd->variant) {
+        const int variant = sd->variant;
+        void* st = stage0 + buf * stage_bytes;
+        switch (variant) {
 #define GB_CASE(F, L)                                                     \
     case variant_id(F, L):                                                \
-        if constexpr (fam_i32(F) == I32) tile_transform<F, L, CTA>(st, xbuf, *ka, np); \
+        if constexpr (fam_i32(F) == I32) tile_transform<F, L, CTA>(st, xbuf, kc, np); \
         break;
             GB_I16_VARIANTS(GB_CASE)
             GB_I32_VARIANTS(GB_CASE)
@@ -124,7 +119,10 @@ __global__ void __launch_bounds__(CTA, I32 ? 2 : 3) k_batch(const BatchDev b, in
             default: break;
         }
         __syncthreads();
+        const long long tnext = sh_next;
+        if (sh_failed) break;
         if (tid == 0) {
+            sh_pending[buf] = 0;
             fence_proxy_async();
             const long long off = lt * P * (long long)sd->n * sd->elem_bytes;
             bulk_store(static_cast<char*>(sd->a.out) + off, st, (unsigned)(np * sd->n * sd->elem_bytes));
@@ -134,10 +132,12 @@ __global__ void __launch_bounds__(CTA, I32 ? 2 : 3) k_batch(const BatchDev b, in
         buf ^= 1;
     }
     if (tid == 0) {
-        if (failed) {
+        if (sh_failed) {
+            atomicMax(&b.ctr[CTR_ERROR], (unsigned long long)BERR_TIMEOUT);
             // let a prefetch that is still in flight land before the CTA leaves (bounded)
+            // (bar[buf]'s parity bit was already advanced past the load it waited for)
             for (int i = 0; i < 2; ++i)
-                if (sh_pending[i]) mbar_wait(&bar[i], phase[i]);
+                if (sh_pending[i]) mbar_wait(&bar[i], ((phases >> i) & 1u) ^ (i == buf ? 1u : 0u));
         }
         bulk_wait_all();
         __threadfence();

@@ -43,6 +43,33 @@ struct KArgs {
     int ftail[16];        // tail matrix [m][k]
 };
 
+// The scalar constants of one design, held in registers while a polynomial is
+// transformed (the matrices stay in parameter or shared memory).
+struct KC {
+    const int2* tab;
+    const int* f8;
+    const int* ftail;
+    int q, c, fneg, wc, canonical, r8_sym, tail_wq, f1, f2, f3;
+};
+
+__device__ __forceinline__ KC make_kc(const KArgs& a) {
+    KC k;
+    k.tab = a.tab;
+    k.f8 = a.f8;
+    k.ftail = a.ftail;
+    k.q = a.q;
+    k.c = a.c;
+    k.fneg = a.fneg;
+    k.wc = a.wc;
+    k.canonical = a.canonical;
+    k.r8_sym = a.r8_sym;
+    k.tail_wq = a.tail_wq;
+    k.f1 = a.f8s[1];
+    k.f2 = a.f8s[2];
+    k.f3 = a.f8s[3];
+    return k;
+}
+
 // ---------------------------------------------------------------------------
 // lane arithmetic
 // ---------------------------------------------------------------------------
@@ -62,10 +89,14 @@ __device__ __forceinline__ int rsz31(long long p) {
 
 __device__ __forceinline__ int wrap16(int x) { return (int)(short)x; }
 
-// partial Barrett reduction, int16: a - round(a c / 2^16) q
-__device__ __forceinline__ int br16(int a, int c, int q) { return wrap16(a - rsz16(a * c) * q); }
-// partial Barrett multiplication, int16: a w - round(a w' / 2^16) q
-__device__ __forceinline__ int bm16(int a, int tw, int wq, int q) { return wrap16(a * tw - rsz16(a * wq) * q); }
+// Partial Barrett reduction / multiplication, int16: a - round(a c / 2^16) q
+// and a w - round(a w' / 2^16) q.  The reference stores both results as int16
+// lanes (a wrap), which never changes them: every multiplier of the tables is
+// within 1.5 of w 2^16 / q (0.5 for the float and constant ones, < 1.5 for
+// round<T>'s truncation of negative values), so for |a| <= 2^15 the quotient
+// error is at most 0.5 + 0.75 and |result| <= 1.25 q < 2^15 for q < 2^16 / 3.
+__device__ __forceinline__ int br16(int a, int c, int q) { return a - rsz16(a * c) * q; }
+__device__ __forceinline__ int bm16(int a, int tw, int wq, int q) { return a * tw - rsz16(a * wq) * q; }
 
 // int32 variants, computed modulo 2^32 like the int32 lanes
 __device__ __forceinline__ int br32(int a, int c, int q) {
@@ -159,7 +190,7 @@ __host__ __device__ constexpr int brev_c(int x) {
 // ---------------------------------------------------------------------------
 
 template <int FAM, int L, int EL, int S>
-__device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const KArgs& a) {
+__device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const KC& a) {
     constexpr int E = 1 << EL;
     constexpr int G = 1 << (L - EL);
     constexpr int LO = window_lo(FAM, L, EL, S);
@@ -246,7 +277,7 @@ __device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const
 #pragma unroll
                 for (int m = 0; m < 8; ++m) x[m] = v[k0 | (m << KB)];
                 if (a.r8_sym) {
-                    const int f1 = a.f8s[1], f2 = a.f8s[2], f3 = a.f8s[3];
+                    const int f1 = a.f1, f2 = a.f2, f3 = a.f3;
                     const int a0 = x[0] + x[4], a1 = x[1] + x[5], a2 = x[2] + x[6], a3 = x[3] + x[7];
                     const int b0 = x[0] - x[4], b1 = x[1] - x[5], b2 = x[2] - x[6], b3 = x[3] - x[7];
                     const int c0 = a0 + a2, c1 = a1 + a3, d0 = a0 - a2, d1 = a1 - a3;
@@ -294,7 +325,7 @@ __device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const
 }
 
 template <int FAM, int L, int EL, int... S>
-__device__ __forceinline__ void run_steps(int (&v)[1 << EL], int* sp, int g, const KArgs& a,
+__device__ __forceinline__ void run_steps(int (&v)[1 << EL], int* sp, int g, const KC& a,
                                           std::integer_sequence<int, S...>) {
     (do_step<FAM, L, EL, S>(v, sp, g, a), ...);
 }
@@ -399,7 +430,7 @@ __device__ __forceinline__ void store_poly(int (&v)[1 << EL], const KArgs& a, lo
 // ---------------------------------------------------------------------------
 
 template <int FAM, int L, int EL, int P, bool BR>
-__global__ void __launch_bounds__(P << (L - EL)) k_ntt(const KArgs a) {
+__global__ void __launch_bounds__(P << (L - EL)) k_ntt(const __grid_constant__ KArgs a) {
     constexpr int G = 1 << (L - EL);
     constexpr int NS = nsteps(FAM, L);
     constexpr int N = 1 << L;
@@ -420,7 +451,8 @@ __global__ void __launch_bounds__(P << (L - EL)) k_ntt(const KArgs a) {
 #pragma unroll
         for (int k = 0; k < (1 << EL); ++k) v[k] = 0;
     }
-    run_steps<FAM, L, EL>(v, sp, g, a, std::make_integer_sequence<int, NS>{});
+    const KC kc = make_kc(a);
+    run_steps<FAM, L, EL>(v, sp, g, kc, std::make_integer_sequence<int, NS>{});
     if (active) store_poly<I32, L, EL, LOZ, BR>(v, a, poly, g);
 }
 

@@ -119,7 +119,7 @@ __device__ __forceinline__ void exchange(int (&v)[1 << EL], int* sp, int g) {
 }
 
 template <int FAM, int L, int CTA>
-__device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KArgs& a, int npolys) {
+__device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KC& a, int npolys) {
     constexpr int EL = batch_el(L);
     constexpr int G = 1 << (L - EL), N = 1 << L, E = 1 << EL;
     constexpr int SW = N + N / 32;
