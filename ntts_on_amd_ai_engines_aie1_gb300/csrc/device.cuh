@@ -166,6 +166,32 @@ __host__ __device__ constexpr int r8_stage_offset(int L, int s) {
 // padded shared-memory index of a position (one spare word every 32)
 __device__ __forceinline__ int spad(int pos) { return pos + (pos >> 5); }
 
+// shared-memory words per polynomial of the exchange buffer (16-byte multiple)
+__host__ __device__ constexpr int xwords(int L) { return (((1 << L) + (1 << L) / 32) + 3) & ~3; }
+
+// Vectorised exchange layout.  When the windows before and after an exchange
+// share position bits [OLO, OLO + VB), the 2^VB values that differ only in
+// those bits stay in one thread on both sides and move as one 8- or 16-byte
+// access.  The word address keeps those bits lowest; the chunk index (the
+// remaining bits) is XOR-folded so that the chunks of a quarter warp spread
+// over all banks.
+template <int OLO, int VB>
+__device__ __forceinline__ int vaddr(int pos) {
+    const int low = (pos >> OLO) & ((1 << VB) - 1);
+    int c = ((pos >> (OLO + VB)) << OLO) | (pos & ((1 << OLO) - 1));
+    if constexpr (VB == 2) c ^= ((c >> 3) ^ (c >> 6) ^ (c >> 9) ^ (c >> 12)) & 7;
+    else c ^= ((c >> 4) ^ (c >> 8) ^ (c >> 12)) & 15;
+    return (c << VB) | low;
+}
+
+template <int G>
+__device__ __forceinline__ void group_sync();
+
+// Moves the thread's registers from the window starting at bit LOA to the
+// window starting at LOB through the shared buffer sp.
+template <int L, int EL, int LOA, int LOB>
+__device__ __forceinline__ void exchange_windows(int (&v)[1 << EL], int* sp, int g);
+
 // position of register k of thread g when the window starts at bit LO
 template <int LO, int EL>
 __device__ __forceinline__ int posmap(int g, int k) {
@@ -176,6 +202,49 @@ template <int G>
 __device__ __forceinline__ void group_sync() {
     if constexpr (G > 32) __syncthreads();
     else __syncwarp();
+}
+
+template <int L, int EL, int LOA, int LOB>
+__device__ __forceinline__ void exchange_windows(int (&v)[1 << EL], int* sp, int g) {
+    constexpr int E = 1 << EL, G = 1 << (L - EL);
+    constexpr int OLO = LOA > LOB ? LOA : LOB;
+    constexpr int OHI = (LOA < LOB ? LOA : LOB) + EL;
+    constexpr int W = OHI > OLO ? OHI - OLO : 0;
+    constexpr int VB = W >= 2 ? 2 : W;
+    group_sync<G>();
+    if constexpr (VB == 0) {
+#pragma unroll
+        for (int k = 0; k < E; ++k) sp[spad(posmap<LOA, EL>(g, k))] = v[k];
+        group_sync<G>();
+#pragma unroll
+        for (int k = 0; k < E; ++k) v[k] = sp[spad(posmap<LOB, EL>(g, k))];
+    } else {
+        constexpr int KA = OLO - LOA, KB = OLO - LOB;   // register bit of the shared bits
+        constexpr int V = 1 << VB;
+#pragma unroll
+        for (int r = 0; r < (E >> VB); ++r) {
+            const int k = ((r >> KA) << (KA + VB)) | (r & ((1 << KA) - 1));
+            const int a = vaddr<OLO, VB>(posmap<LOA, EL>(g, k));
+            if constexpr (V == 4)
+                *reinterpret_cast<int4*>(sp + a) =
+                    make_int4(v[k], v[k | (1 << KA)], v[k | (2 << KA)], v[k | (3 << KA)]);
+            else
+                *reinterpret_cast<int2*>(sp + a) = make_int2(v[k], v[k | (1 << KA)]);
+        }
+        group_sync<G>();
+#pragma unroll
+        for (int r = 0; r < (E >> VB); ++r) {
+            const int k = ((r >> KB) << (KB + VB)) | (r & ((1 << KB) - 1));
+            const int a = vaddr<OLO, VB>(posmap<LOB, EL>(g, k));
+            if constexpr (V == 4) {
+                const int4 w = *reinterpret_cast<const int4*>(sp + a);
+                v[k] = w.x; v[k | (1 << KB)] = w.y; v[k | (2 << KB)] = w.z; v[k | (3 << KB)] = w.w;
+            } else {
+                const int2 w = *reinterpret_cast<const int2*>(sp + a);
+                v[k] = w.x; v[k | (1 << KB)] = w.y;
+            }
+        }
+    }
 }
 
 template <int NB>
@@ -200,14 +269,7 @@ __device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const
     static_assert(B >= LO && B + W <= LO + EL, "step outside its window");
     if constexpr (S > 0) {
         constexpr int PLO = window_lo(FAM, L, EL, S - 1);
-        if constexpr (PLO != LO) {
-            group_sync<G>();
-#pragma unroll
-            for (int k = 0; k < E; ++k) sp[spad(posmap<PLO, EL>(g, k))] = v[k];
-            group_sync<G>();
-#pragma unroll
-            for (int k = 0; k < E; ++k) v[k] = sp[spad(posmap<LO, EL>(g, k))];
-        }
+        if constexpr (PLO != LO) exchange_windows<L, EL, PLO, LO>(v, sp, g);
     }
     const int q = a.q;
 #pragma unroll
@@ -434,7 +496,7 @@ __global__ void __launch_bounds__(P << (L - EL)) k_ntt(const __grid_constant__ K
     constexpr int G = 1 << (L - EL);
     constexpr int NS = nsteps(FAM, L);
     constexpr int N = 1 << L;
-    constexpr int SW = N + N / 32;
+    constexpr int SW = xwords(L);
     constexpr bool I32 = fam_i32(FAM);
     extern __shared__ int smem[];
     const int tid = threadIdx.x;
@@ -477,9 +539,7 @@ __host__ __device__ constexpr int choose_polys(int fam, int L) {
     return p < 1 ? 1 : p;
 }
 __host__ __device__ constexpr int smem_bytes(int fam, int L) {
-    return num_windows(fam, L, choose_el(fam, L)) > 1
-               ? choose_polys(fam, L) * ((1 << L) + (1 << L) / 32) * 4
-               : 0;
+    return num_windows(fam, L, choose_el(fam, L)) > 1 ? choose_polys(fam, L) * xwords(L) * 4 : 0;
 }
 
 template <int FAM, int L, bool BR>

@@ -107,22 +107,11 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 // one tile: P polynomials staged contiguously in shared memory
 // ---------------------------------------------------------------------------
 
-template <int L, int EL, int LOA, int LOB>
-__device__ __forceinline__ void exchange(int (&v)[1 << EL], int* sp, int g) {
-    constexpr int E = 1 << EL, G = 1 << (L - EL);
-    group_sync<G>();
-#pragma unroll
-    for (int k = 0; k < E; ++k) sp[spad(posmap<LOA, EL>(g, k))] = v[k];
-    group_sync<G>();
-#pragma unroll
-    for (int k = 0; k < E; ++k) v[k] = sp[spad(posmap<LOB, EL>(g, k))];
-}
-
 template <int FAM, int L, int CTA>
 __device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KC& a, int npolys) {
     constexpr int EL = batch_el(L);
     constexpr int G = 1 << (L - EL), N = 1 << L, E = 1 << EL;
-    constexpr int SW = N + N / 32;
+    constexpr int SW = xwords(L);
     constexpr int NS = nsteps(FAM, L);
     constexpr int LOS = L - EL;                          // staging layout: strided, conflict-free
     constexpr int LO0 = window_lo(FAM, L, EL, 0);
@@ -148,7 +137,7 @@ __device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KC&
 #pragma unroll
         for (int k = 0; k < E; ++k) v[k] = 0;
     }
-    if constexpr (LO0 != LOS) exchange<L, EL, LOS, LO0>(v, sp, g);
+    if constexpr (LO0 != LOS) exchange_windows<L, EL, LOS, LO0>(v, sp, g);
     run_steps<FAM, L, EL>(v, sp, g, a, std::make_integer_sequence<int, NS>{});
     if (a.canonical) {
 #pragma unroll
@@ -190,7 +179,7 @@ __host__ __device__ constexpr int batch_stage_bytes(int cta, int L, int elem) {
     return cta * (1 << batch_el(L)) * elem;
 }
 __host__ __device__ constexpr int batch_xbuf_bytes(int cta, int L) {
-    return batch_el(L) == L ? 0 : (cta >> (L - batch_el(L))) * ((1 << L) + (1 << L) / 32) * 4;
+    return batch_el(L) == L ? 0 : (cta >> (L - batch_el(L))) * xwords(L) * 4;
 }
 
 }  // namespace gbntt
