@@ -198,15 +198,25 @@ int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t
             return cuda_fail(e, "cudaFuncSetAttribute");
         }
     }
-    if (!hp.tab.empty()) {
-        p->tab_bytes = hp.tab.size() * sizeof(int32_t);
+    // int16 radix-2/4 designs: (tw, w') packed into one word (both fit int16)
+    const bool packed = (p->fam == F_R2F16 || p->fam == F_R2I16 || p->fam == F_R4F16);
+    std::vector<int32_t> dev_tab;
+    if (packed) {
+        dev_tab.resize(hp.tab.size() / 2);
+        for (size_t i = 0; i < dev_tab.size(); ++i)
+            dev_tab[i] = (int32_t)(((uint32_t)hp.tab[2 * i] & 0xFFFFu) | ((uint32_t)hp.tab[2 * i + 1] << 16));
+    } else {
+        dev_tab = hp.tab;
+    }
+    if (!dev_tab.empty()) {
+        p->tab_bytes = dev_tab.size() * sizeof(int32_t);
         e = cudaMalloc(&p->d_tab, p->tab_bytes);
         if (e != cudaSuccess) {
             delete p;
             return e == cudaErrorMemoryAllocation ? fail(GBNTT_ERR_NOMEM, "device allocation failed")
                                                   : cuda_fail(e, "cudaMalloc");
         }
-        e = cudaMemcpy(p->d_tab, hp.tab.data(), p->tab_bytes, cudaMemcpyHostToDevice);
+        e = cudaMemcpy(p->d_tab, dev_tab.data(), p->tab_bytes, cudaMemcpyHostToDevice);
         if (e != cudaSuccess) {
             cudaFree(p->d_tab);
             delete p;
@@ -215,7 +225,9 @@ int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t
     }
     KArgs& a = p->base;
     std::memset(&a, 0, sizeof(a));
-    a.tab = p->d_tab;
+    a.tab = packed ? nullptr : p->d_tab;
+    a.tab16 = packed ? reinterpret_cast<const int*>(p->d_tab) : nullptr;
+    a.wq1 = (p->fam == F_R4F16 && hp.tab.size() >= 2) ? hp.tab[1] : 0;
     a.q = (int)hp.q;
     a.c = hp.c;
     a.fneg = hp.r4_fneg;

@@ -31,7 +31,9 @@ struct KArgs {
     const void* in;
     void* out;
     long long batch;
-    const int2* tab;      // (tw, w') pairs of the design
+    const int2* tab;      // (tw, w') pairs of the design (int32 designs, radix-8)
+    const int* tab16;     // int16 designs: tw | w' << 16 packed in one word
+    int wq1;              // radix-4: multiplier of the twiddle 1 (table entry 0)
     int q;
     int c;                // Barrett constant of the reduction (K = 16 or 32)
     int fneg, wc;         // radix-4 omega_4 and its multiplier
@@ -47,14 +49,17 @@ struct KArgs {
 // transformed (the matrices stay in parameter or shared memory).
 struct KC {
     const int2* tab;
+    const int* tab16;
     const int* f8;
     const int* ftail;
-    int q, c, fneg, wc, canonical, r8_sym, tail_wq, f1, f2, f3;
+    int q, c, fneg, wc, canonical, r8_sym, tail_wq, f1, f2, f3, wq1;
 };
 
 __device__ __forceinline__ KC make_kc(const KArgs& a) {
     KC k;
     k.tab = a.tab;
+    k.tab16 = a.tab16;
+    k.wq1 = a.wq1;
     k.f8 = a.f8;
     k.ftail = a.ftail;
     k.q = a.q;
@@ -88,6 +93,9 @@ __device__ __forceinline__ int rsz31(long long p) {
 }
 
 __device__ __forceinline__ int wrap16(int x) { return (int)(short)x; }
+// halves of a packed (tw | w' << 16) table word
+__device__ __forceinline__ int lo16(int w) { return (int)(short)w; }
+__device__ __forceinline__ int hi16(int w) { return w >> 16; }
 
 // Partial Barrett reduction / multiplication, int16: a - round(a c / 2^16) q
 // and a w - round(a w' / 2^16) q.  The reference stores both results as int16
@@ -280,12 +288,13 @@ __device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const
             // ntt_r2_kernels.cc:434-472, ntt_r2_int32_kernels.cc:267-295)
             const int k1 = k0 | (1 << KB);
             const int blk = posmap<LO, EL>(g, k0) >> (B + 1);
-            const int2 t = __ldg(&a.tab[blk]);
             if constexpr (FAM == F_R2F16) {
-                const int u = br16(v[k0], a.c, q), w = bm16(v[k1], t.x, t.y, q);
+                const int t = __ldg(&a.tab16[blk]);
+                const int u = br16(v[k0], a.c, q), w = bm16(v[k1], lo16(t), hi16(t), q);
                 v[k0] = wrap16(u + w);
                 v[k1] = wrap16(u - w);
             } else {
+                const int2 t = __ldg(&a.tab[blk]);
                 const int u = br32(v[k0], a.c, q), w = bm32(v[k1], t.x, t.y, q);
                 v[k0] = add32(u, w);
                 v[k1] = sub32(u, w);
@@ -307,22 +316,32 @@ __device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const
                 v[k1] = d;
             } else {
                 const int tpos = posmap<LO, EL>(g, k0) & ((1 << B) - 1);
-                const int2 t = __ldg(&a.tab[(1 << B) + tpos]);
-                const int u = br16(v[k0], a.c, q), w = bm16(v[k1], t.x, t.y, q);
+                const int t = __ldg(&a.tab16[(1 << B) + tpos]);
+                const int u = br16(v[k0], a.c, q), w = bm16(v[k1], lo16(t), hi16(t), q);
                 v[k0] = wrap16(u + w);
                 v[k1] = wrap16(u - w);
             }
         } else if constexpr (FAM == F_R4F16) {
             // radix-4 layer S (ntt_r4_kernels.cc:243-261)
+            // input 0 always has twiddle 1 (power 0), and so has every input
+            // of stage 0 (block 0): those products are plain reductions with
+            // the multiplier of 1, read from table entry 0.
             constexpr int OFF = 4 * (((1 << (2 * S)) - 1) / 3);
-            const int blk = posmap<LO, EL>(g, k0) >> (B + 2);
-            const int4* t4 = reinterpret_cast<const int4*>(a.tab + OFF + 4 * blk);
-            const int4 t01 = __ldg(t4), t23 = __ldg(t4 + 1);
             const int ka = k0, kb1 = k0 | (1 << KB), kb2 = k0 | (2 << KB), kb3 = k0 | (3 << KB);
-            const int A0 = bm16(v[ka], t01.x, t01.y, q);
-            const int A1 = bm16(v[kb1], t01.z, t01.w, q);
-            const int A2 = bm16(v[kb2], t23.x, t23.y, q);
-            const int A3 = bm16(v[kb3], t23.z, t23.w, q);
+            int A0, A1, A2, A3;
+            if constexpr (S == 0) {
+                A0 = br16(v[ka], a.wq1, q);
+                A1 = br16(v[kb1], a.wq1, q);
+                A2 = br16(v[kb2], a.wq1, q);
+                A3 = br16(v[kb3], a.wq1, q);
+            } else {
+                const int blk = posmap<LO, EL>(g, k0) >> (B + 2);
+                const int4 t = __ldg(reinterpret_cast<const int4*>(a.tab16 + OFF + 4 * blk));
+                A0 = br16(v[ka], hi16(t.x), q);
+                A1 = bm16(v[kb1], lo16(t.y), hi16(t.y), q);
+                A2 = bm16(v[kb2], lo16(t.z), hi16(t.z), q);
+                A3 = bm16(v[kb3], lo16(t.w), hi16(t.w), q);
+            }
             const int A5 = bm16(A1, a.fneg, a.wc, q);
             const int A6 = bm16(A3, a.fneg, a.wc, q);
             v[ka] = wrap16(A0 + A1 + A2 + A3);
