@@ -143,6 +143,11 @@ typedef struct gbntt_segment {
 
 typedef struct gbntt_batch gbntt_batch;
 
+/* flags: GBNTT_BATCH_NO_TUNE skips the autotuner, which otherwise times every
+ * persistent-kernel configuration (coefficients per thread, hence threads
+ * and CTAs per transform and polynomials per tile) on the batch itself at
+ * creation and keeps the fastest.  Creation then writes the segments' outputs. */
+#define GBNTT_BATCH_NO_TUNE 0x1u
 int gbntt_batch_create(gbntt_batch** batch, const gbntt_segment* segs, uint32_t nsegs, uint32_t flags);
 int gbntt_batch_execute(gbntt_batch* batch, void* stream);
 /* The same launches captured once in a CUDA graph and replayed. */
@@ -160,6 +165,7 @@ int gbntt_batch_status(gbntt_batch* batch);
 #define GBNTT_BQ_TILES    1   /* tiles of the persistent launches        */
 #define GBNTT_BQ_GRID     2   /* CTAs of the largest persistent launch   */
 #define GBNTT_BQ_SMEM     3   /* dynamic shared memory per CTA (bytes)   */
+#define GBNTT_BQ_EL16     4   /* log2 coefficients per thread chosen for the int16 launch */
 int gbntt_batch_query(const gbntt_batch* batch, int what, int64_t* value);
 int gbntt_batch_destroy(gbntt_batch* batch);
 

@@ -29,8 +29,8 @@ namespace {
 
 constexpr int SMEM_HEADER = 1024;   // mbarriers + the current segment's KArgs
 
-template <bool I32, int CTA>
-__global__ void __launch_bounds__(CTA, I32 ? 2 : 3) k_batch(const BatchDev b, int stage_bytes) {
+template <bool I32, int CTA, int ELMAX>
+__global__ void __launch_bounds__(CTA, (I32 || ELMAX > 5) ? 2 : 3) k_batch(const BatchDev b, int stage_bytes) {
     extern __shared__ __align__(128) unsigned char smem[];
     unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem);
     KArgs* ka = reinterpret_cast<KArgs*>(smem + 64);
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(CTA, I32 ? 2 : 3) k_batch(const BatchDev b, in
         switch (variant) {
 #define GB_CASE(F, L)                                                     \
     case variant_id(F, L):                                                \
-        if constexpr (fam_i32(F) == I32) tile_transform<F, L, CTA>(st, xbuf, kc, np); \
+        if constexpr (fam_i32(F) == I32) tile_transform<F, L, CTA, ELMAX>(st, xbuf, kc, np); \
         break;
             GB_I16_VARIANTS(GB_CASE)
             GB_I32_VARIANTS(GB_CASE)
@@ -162,22 +162,37 @@ constexpr int BATCH_CTA = 256;
 
 }  // namespace
 
-const void* batch_kernel(bool i32) {
-    return i32 ? reinterpret_cast<const void*>(&k_batch<true, BATCH_CTA>)
-               : reinterpret_cast<const void*>(&k_batch<false, BATCH_CTA>);
-}
+// persistent-kernel configurations: (storage type, coefficients per thread)
+struct BatchConfig {
+    bool i32;
+    int elmax;
+    const void* fn;
+};
+
+static const BatchConfig kConfigs[] = {
+    {false, 6, reinterpret_cast<const void*>(&k_batch<false, BATCH_CTA, 6>)},
+    {false, 5, reinterpret_cast<const void*>(&k_batch<false, BATCH_CTA, 5>)},
+    {true, 5, reinterpret_cast<const void*>(&k_batch<true, BATCH_CTA, 5>)},
+};
 
 }  // namespace gbntt
 
 using namespace gbntt;
 
 struct gbntt_batch {
-    struct Part {                       // one persistent launch (int16 or int32 segments)
-        bool i32 = false;
+    struct Layout {                     // one configuration of one persistent launch
+        int cfg = -1;                   // index into kConfigs
         std::vector<SegDev> segs;
         SegDev* d_segs = nullptr;
         long long total_tiles = 0;
         int stage_bytes = 0, smem = 0, grid = 0;
+        float ms = -1.f;                // autotuner timing
+    };
+    struct Part {                       // the int16 or the int32 segments
+        bool i32 = false;
+        std::vector<Layout> layouts;    // candidate configurations
+        int chosen = 0;
+        std::vector<int> user_index;    // caller's segment of each SegDev
     };
     Part parts[2];
     int nparts = 0;
@@ -186,27 +201,32 @@ struct gbntt_batch {
     std::vector<gbntt_segment> user;    // the caller's segments
     unsigned long long* d_ctr = nullptr;   // CTR_WORDS per part
     cudaGraphExec_t graph = nullptr;
-    cudaStream_t graph_stream = nullptr;
 };
 
 namespace {
 
 int batch_fail(int code, const std::string& msg) { return gbntt_internal_fail(code, msg); }
 
+int launch_layout(gbntt_batch* b, int pi, const gbntt_batch::Layout& lay, cudaStream_t s) {
+    if (lay.total_tiles == 0) return GBNTT_OK;
+    BatchDev bd;
+    bd.segs = lay.d_segs;
+    bd.nsegs = (int)lay.segs.size();
+    bd.total_tiles = lay.total_tiles;
+    bd.ctr = b->d_ctr + CTR_WORDS * pi;
+    int sb = lay.stage_bytes;
+    void* args[] = {&bd, &sb};
+    cudaError_t e = cudaLaunchKernel(kConfigs[lay.cfg].fn, dim3(lay.grid), dim3(BATCH_CTA), args, lay.smem, s);
+    if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
+    gbntt_internal_count_launch();
+    return GBNTT_OK;
+}
+
 int launch_batch(gbntt_batch* b, cudaStream_t s) {
     for (int i = 0; i < b->nparts; ++i) {
         auto& p = b->parts[i];
-        if (p.total_tiles == 0) continue;
-        BatchDev bd;
-        bd.segs = p.d_segs;
-        bd.nsegs = (int)p.segs.size();
-        bd.total_tiles = p.total_tiles;
-        bd.ctr = b->d_ctr + CTR_WORDS * i;
-        int sb = p.stage_bytes;
-        void* args[] = {&bd, &sb};
-        cudaError_t e = cudaLaunchKernel(batch_kernel(p.i32), dim3(p.grid), dim3(BATCH_CTA), args, p.smem, s);
-        if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
-        gbntt_internal_count_launch();
+        const int rc = launch_layout(b, i, p.layouts[p.chosen], s);
+        if (rc != GBNTT_OK) return rc;
     }
     for (size_t k = 0; k < b->user.size(); ++k) {
         if (b->part_of[k] >= 0) continue;
@@ -217,12 +237,45 @@ int launch_batch(gbntt_batch* b, cudaStream_t s) {
     return GBNTT_OK;
 }
 
+// Times every candidate configuration of every part on the batch itself (the
+// outputs it writes are the batch's own results) and keeps the fastest.
+int autotune(gbntt_batch* b) {
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+        return batch_fail(GBNTT_ERR_CUDA, "autotune stream");
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int rc = GBNTT_OK;
+    for (int i = 0; i < b->nparts && rc == GBNTT_OK; ++i) {
+        auto& p = b->parts[i];
+        if (p.layouts.size() < 2) continue;
+        for (size_t c = 0; c < p.layouts.size() && rc == GBNTT_OK; ++c) {
+            for (int w = 0; w < 2 && rc == GBNTT_OK; ++w) rc = launch_layout(b, i, p.layouts[c], s);
+            cudaEventRecord(e0, s);
+            for (int w = 0; w < 5 && rc == GBNTT_OK; ++w) rc = launch_layout(b, i, p.layouts[c], s);
+            cudaEventRecord(e1, s);
+            if (cudaEventSynchronize(e1) != cudaSuccess) rc = batch_fail(GBNTT_ERR_CUDA, "autotune timing");
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            p.layouts[c].ms = ms / 5.f;
+        }
+        size_t best = 0;
+        for (size_t c = 1; c < p.layouts.size(); ++c)
+            if (p.layouts[c].ms >= 0.f && p.layouts[c].ms < p.layouts[best].ms) best = c;
+        p.chosen = (int)best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(s);
+    return rc;
+}
+
 }  // namespace
 
 extern "C" {
 
 int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t nsegs, uint32_t flags) {
-    (void)flags;
     if (!out || (!segs && nsegs)) return batch_fail(GBNTT_ERR_ARG, "null argument");
     *out = nullptr;
     gbntt_batch* b = new gbntt_batch();
@@ -253,50 +306,61 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
         if (id < 0) {
             id = b->nparts++;
             b->parts[id].i32 = i32;
+            for (int c = 0; c < (int)(sizeof(kConfigs) / sizeof(kConfigs[0])); ++c)
+                if (kConfigs[c].i32 == i32) {
+                    gbntt_batch::Layout lay;
+                    lay.cfg = c;
+                    b->parts[id].layouts.push_back(lay);
+                }
         }
         auto& part = b->parts[id];
-        SegDev sd;
-        std::memset(&sd, 0, sizeof(sd));
-        sd.a = a;
-        sd.a.in = u.d_in;
-        sd.a.out = u.d_out;
-        sd.a.batch = (long long)u.count;
-        sd.n = 1 << L;
-        sd.elem_bytes = eb;
-        sd.variant = variant_id(fam, L);
-        const int G = 1 << (L - batch_el(L));
-        sd.polys_per_tile = BATCH_CTA / G;
-        sd.tiles = ((long long)u.count + sd.polys_per_tile - 1) / sd.polys_per_tile;
-        sd.tile0 = part.total_tiles;
-        part.total_tiles += sd.tiles;
-        part.stage_bytes = std::max(part.stage_bytes, batch_stage_bytes(BATCH_CTA, L, eb));
-        part.smem = std::max(part.smem, batch_xbuf_bytes(BATCH_CTA, L));
         b->part_of[k] = id;
-        b->index_in_part[k] = (int)part.segs.size();
-        part.segs.push_back(sd);
+        b->index_in_part[k] = (int)part.user_index.size();
+        part.user_index.push_back(k);
+        for (auto& lay : part.layouts) {
+            const int elmax = kConfigs[lay.cfg].elmax;
+            SegDev sd;
+            std::memset(&sd, 0, sizeof(sd));
+            sd.a = a;
+            sd.a.in = u.d_in;
+            sd.a.out = u.d_out;
+            sd.a.batch = (long long)u.count;
+            sd.n = 1 << L;
+            sd.elem_bytes = eb;
+            sd.variant = variant_id(fam, L);
+            const int G = 1 << (L - batch_el(L, elmax));
+            sd.polys_per_tile = BATCH_CTA / G;
+            sd.tiles = ((long long)u.count + sd.polys_per_tile - 1) / sd.polys_per_tile;
+            sd.tile0 = lay.total_tiles;
+            lay.total_tiles += sd.tiles;
+            lay.stage_bytes = std::max(lay.stage_bytes, batch_stage_bytes(BATCH_CTA, L, eb, elmax));
+            lay.smem = std::max(lay.smem, batch_xbuf_bytes(BATCH_CTA, L, elmax));
+            lay.segs.push_back(sd);
+        }
     }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     for (int i = 0; i < b->nparts; ++i) {
-        auto& p = b->parts[i];
-        p.stage_bytes = (p.stage_bytes + 127) & ~127;
-        p.smem = SMEM_HEADER + 2 * p.stage_bytes + p.smem;
-        const void* fn = batch_kernel(p.i32);
-        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem);
-        int per_sm = 0;
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BATCH_CTA, p.smem);
-        if (e != cudaSuccess || per_sm < 1) {
-            gbntt_batch_destroy(b);
-            return batch_fail(GBNTT_ERR_CUDA, std::string("batch kernel configuration: ") + cudaGetErrorString(e));
-        }
-        p.grid = (int)std::min<long long>((long long)per_sm * sms, p.total_tiles);
-        e = cudaMalloc(&p.d_segs, sizeof(SegDev) * p.segs.size());
-        if (e == cudaSuccess)
-            e = cudaMemcpy(p.d_segs, p.segs.data(), sizeof(SegDev) * p.segs.size(), cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) {
-            gbntt_batch_destroy(b);
-            return batch_fail(GBNTT_ERR_NOMEM, "batch descriptor allocation failed");
+        for (auto& lay : b->parts[i].layouts) {
+            lay.stage_bytes = (lay.stage_bytes + 127) & ~127;
+            lay.smem = SMEM_HEADER + 2 * lay.stage_bytes + lay.smem;
+            const void* fn = kConfigs[lay.cfg].fn;
+            cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, lay.smem);
+            int per_sm = 0;
+            if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BATCH_CTA, lay.smem);
+            if (e != cudaSuccess || per_sm < 1) {
+                gbntt_batch_destroy(b);
+                return batch_fail(GBNTT_ERR_CUDA, std::string("batch kernel configuration: ") + cudaGetErrorString(e));
+            }
+            lay.grid = (int)std::min<long long>((long long)per_sm * sms, lay.total_tiles);
+            e = cudaMalloc(&lay.d_segs, sizeof(SegDev) * lay.segs.size());
+            if (e == cudaSuccess)
+                e = cudaMemcpy(lay.d_segs, lay.segs.data(), sizeof(SegDev) * lay.segs.size(), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) {
+                gbntt_batch_destroy(b);
+                return batch_fail(GBNTT_ERR_NOMEM, "batch descriptor allocation failed");
+            }
         }
     }
     cudaError_t e = cudaMalloc(&b->d_ctr, sizeof(unsigned long long) * CTR_WORDS * 2);
@@ -304,6 +368,13 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
     if (e != cudaSuccess) {
         gbntt_batch_destroy(b);
         return batch_fail(GBNTT_ERR_NOMEM, "batch scratch allocation failed");
+    }
+    if (!(flags & GBNTT_BATCH_NO_TUNE)) {
+        const int rc = autotune(b);
+        if (rc != GBNTT_OK) {
+            gbntt_batch_destroy(b);
+            return rc;
+        }
     }
     *out = b;
     return GBNTT_OK;
@@ -340,33 +411,34 @@ int gbntt_batch_graph_launch(gbntt_batch* b, void* stream) {
     cudaError_t e = cudaGraphLaunch(b->graph, s);
     if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
     for (int i = 0; i < b->nparts; ++i)
-        if (b->parts[i].total_tiles) gbntt_internal_count_launch();
+        if (b->parts[i].layouts[b->parts[i].chosen].total_tiles) gbntt_internal_count_launch();
+    for (size_t k = 0; k < b->user.size(); ++k)
+        if (b->part_of[k] < 0 && b->user[k].count) gbntt_internal_count_launch();
     return GBNTT_OK;
 }
 
 int gbntt_batch_execute_host(gbntt_batch* b, const void* const* h_in, void* const* h_out, void* stream) {
     if (!b || !h_in || !h_out) return batch_fail(GBNTT_ERR_ARG, "null argument");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    for (size_t k = 0; k < b->user.size(); ++k) {
+    auto bytes_of = [&](size_t k) {
         const gbntt_segment& u = b->user[k];
         int64_t n = 0, eb = 0;
         gbntt_plan_query(u.plan, GBNTT_Q_N, &n);
         gbntt_plan_query(u.plan, GBNTT_Q_ELEM_BYTES, &eb);
-        const size_t bytes = (size_t)u.count * (size_t)n * (size_t)eb;
+        return (size_t)u.count * (size_t)n * (size_t)eb;
+    };
+    for (size_t k = 0; k < b->user.size(); ++k) {
+        const size_t bytes = bytes_of(k);
         if (!bytes) continue;
-        cudaError_t e = cudaMemcpyAsync(const_cast<void*>(u.d_in), h_in[k], bytes, cudaMemcpyHostToDevice, s);
+        cudaError_t e = cudaMemcpyAsync(const_cast<void*>(b->user[k].d_in), h_in[k], bytes, cudaMemcpyHostToDevice, s);
         if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("H2D: ") + cudaGetErrorString(e));
     }
     int rc = gbntt_batch_graph_launch(b, stream);
     if (rc != GBNTT_OK) return rc;
     for (size_t k = 0; k < b->user.size(); ++k) {
-        const gbntt_segment& u = b->user[k];
-        int64_t n = 0, eb = 0;
-        gbntt_plan_query(u.plan, GBNTT_Q_N, &n);
-        gbntt_plan_query(u.plan, GBNTT_Q_ELEM_BYTES, &eb);
-        const size_t bytes = (size_t)u.count * (size_t)n * (size_t)eb;
+        const size_t bytes = bytes_of(k);
         if (!bytes) continue;
-        cudaError_t e = cudaMemcpyAsync(h_out[k], u.d_out, bytes, cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaMemcpyAsync(h_out[k], b->user[k].d_out, bytes, cudaMemcpyDeviceToHost, s);
         if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("D2H: ") + cudaGetErrorString(e));
     }
     cudaError_t e = cudaStreamSynchronize(s);
@@ -383,12 +455,14 @@ int gbntt_batch_set_io(gbntt_batch* b, uint32_t seg, const void* d_in, void* d_o
     b->user[seg].d_in = d_in;
     b->user[seg].d_out = d_out;
     if (pi >= 0) {
-        auto& p = b->parts[pi];
-        SegDev& sd = p.segs[b->index_in_part[seg]];
-        sd.a.in = d_in;
-        sd.a.out = d_out;
-        cudaError_t e = cudaMemcpy(p.d_segs + b->index_in_part[seg], &sd, sizeof(SegDev), cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, "descriptor update failed");
+        const int j = b->index_in_part[seg];
+        for (auto& lay : b->parts[pi].layouts) {
+            SegDev& sd = lay.segs[j];
+            sd.a.in = d_in;
+            sd.a.out = d_out;
+            cudaError_t e = cudaMemcpy(lay.d_segs + j, &sd, sizeof(SegDev), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, "descriptor update failed");
+        }
     } else if (b->graph) {
         cudaGraphExecDestroy(b->graph);   // per-plan launches captured the old pointers
         b->graph = nullptr;
@@ -411,23 +485,19 @@ int gbntt_batch_status(gbntt_batch* b) {
 int gbntt_batch_query(const gbntt_batch* b, int what, int64_t* value) {
     if (!b || !value) return batch_fail(GBNTT_ERR_ARG, "null argument");
     int64_t v = 0;
-    switch (what) {
-    case GBNTT_BQ_LAUNCHES:
-        for (int i = 0; i < b->nparts; ++i) v += b->parts[i].total_tiles ? 1 : 0;
-        for (size_t k = 0; k < b->user.size(); ++k) v += b->part_of[k] < 0 ? 1 : 0;
-        break;
-    case GBNTT_BQ_TILES:
-        for (int i = 0; i < b->nparts; ++i) v += b->parts[i].total_tiles;
-        break;
-    case GBNTT_BQ_GRID:
-        for (int i = 0; i < b->nparts; ++i) v = std::max<int64_t>(v, b->parts[i].grid);
-        break;
-    case GBNTT_BQ_SMEM:
-        for (int i = 0; i < b->nparts; ++i) v = std::max<int64_t>(v, b->parts[i].smem);
-        break;
-    default:
-        return batch_fail(GBNTT_ERR_ARG, "unknown query");
+    for (int i = 0; i < b->nparts; ++i) {
+        const auto& lay = b->parts[i].layouts[b->parts[i].chosen];
+        switch (what) {
+        case GBNTT_BQ_LAUNCHES: v += lay.total_tiles ? 1 : 0; break;
+        case GBNTT_BQ_TILES: v += lay.total_tiles; break;
+        case GBNTT_BQ_GRID: v = std::max<int64_t>(v, lay.grid); break;
+        case GBNTT_BQ_SMEM: v = std::max<int64_t>(v, lay.smem); break;
+        case GBNTT_BQ_EL16: if (!b->parts[i].i32) v = kConfigs[lay.cfg].elmax; break;
+        default: return batch_fail(GBNTT_ERR_ARG, "unknown query");
+        }
     }
+    if (what == GBNTT_BQ_LAUNCHES)
+        for (size_t k = 0; k < b->user.size(); ++k) v += (b->part_of[k] < 0 && b->user[k].count) ? 1 : 0;
     *value = v;
     return GBNTT_OK;
 }
@@ -436,7 +506,8 @@ int gbntt_batch_destroy(gbntt_batch* b) {
     if (!b) return GBNTT_OK;
     if (b->graph) cudaGraphExecDestroy(b->graph);
     for (int i = 0; i < b->nparts; ++i)
-        if (b->parts[i].d_segs) cudaFree(b->parts[i].d_segs);
+        for (auto& lay : b->parts[i].layouts)
+            if (lay.d_segs) cudaFree(lay.d_segs);
     if (b->d_ctr) cudaFree(b->d_ctr);
     delete b;
     return GBNTT_OK;

@@ -41,8 +41,8 @@ struct BatchDev {
     unsigned long long* ctr;   // CTR_WORDS scratch words, zero between launches
 };
 
-constexpr int BATCH_EL = 5;
-__host__ __device__ constexpr int batch_el(int L) { return L < BATCH_EL ? L : BATCH_EL; }
+// coefficients per thread (log2) of a persistent-kernel configuration
+__host__ __device__ constexpr int batch_el(int L, int elmax) { return L < elmax ? L : elmax; }
 __host__ __device__ constexpr int variant_id(int fam, int L) { return (fam << 4) | L; }
 
 // ---------------------------------------------------------------------------
@@ -107,9 +107,9 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 // one tile: P polynomials staged contiguously in shared memory
 // ---------------------------------------------------------------------------
 
-template <int FAM, int L, int CTA>
+template <int FAM, int L, int CTA, int ELMAX>
 __device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KC& a, int npolys) {
-    constexpr int EL = batch_el(L);
+    constexpr int EL = batch_el(L, ELMAX);
     constexpr int G = 1 << (L - EL), N = 1 << L, E = 1 << EL;
     constexpr int SW = xwords(L);
     constexpr int NS = nsteps(FAM, L);
@@ -174,12 +174,12 @@ __device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KC&
 }
 
 // shared-memory bytes the persistent kernel needs for the largest variant of a batch
-__host__ __device__ constexpr int batch_stage_bytes(int cta, int L, int elem) {
+__host__ __device__ constexpr int batch_stage_bytes(int cta, int L, int elem, int elmax) {
     // P * N = cta * E coefficients per tile
-    return cta * (1 << batch_el(L)) * elem;
+    return cta * (1 << batch_el(L, elmax)) * elem;
 }
-__host__ __device__ constexpr int batch_xbuf_bytes(int cta, int L) {
-    return batch_el(L) == L ? 0 : (cta >> (L - batch_el(L))) * xwords(L) * 4;
+__host__ __device__ constexpr int batch_xbuf_bytes(int cta, int L, int elmax) {
+    return batch_el(L, elmax) == L ? 0 : (cta >> (L - batch_el(L, elmax))) * xwords(L) * 4;
 }
 
 }  // namespace gbntt

@@ -105,4 +105,8 @@ def test_batch_counts_launches(gb):
     b.execute()
     torch.cuda.synchronize()
     assert gb.launch_count() == c0 + 1
-    assert b.tiles == 4096 // 8
+    el = b.query(4)                       # coefficients per thread chosen by the autotuner
+    assert el in (5, 6)
+    assert b.tiles == 4096 // (256 >> (10 - el))
+    b2 = gb.Batch([(plan, x, y)], flags=1)   # autotuner off
+    assert b2.query(4) == 6
