@@ -166,6 +166,7 @@ int gbntt_batch_status(gbntt_batch* batch);
 #define GBNTT_BQ_GRID     2   /* CTAs of the largest persistent launch   */
 #define GBNTT_BQ_SMEM     3   /* dynamic shared memory per CTA (bytes)   */
 #define GBNTT_BQ_EL16     4   /* log2 coefficients per thread chosen for the int16 launch */
+#define GBNTT_BQ_FAMSET   5   /* design families compiled into the chosen int16 kernel (bit mask) */
 int gbntt_batch_query(const gbntt_batch* batch, int what, int64_t* value);
 int gbntt_batch_destroy(gbntt_batch* batch);
 

@@ -1,195 +1,36 @@
-// batch.cu -- persistent batched launches (gbntt_batch_* in include/gb300_ntt.h).
+// batch.cu -- persistent batched launches (gbntt_batch_* in include/gb300_ntt.h):
+// segment descriptors, tile order, configuration autotuning, graph replay.
 #include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "../../include/gb300_ntt.h"
-#include "persist.cuh"
+#include "batch_kernel.cuh"
 #include "plan_internal.h"
 
-namespace gbntt {
+using namespace gbntt;
 
-namespace {
-
-// every (family, L) the persistent kernels implement, per storage type
-#define GB_I16_VARIANTS(X)                                                                                   \
-    X(F_R2F16, 3) X(F_R2F16, 4) X(F_R2F16, 5) X(F_R2F16, 6) X(F_R2F16, 7) X(F_R2F16, 8) X(F_R2F16, 9)         \
-    X(F_R2F16, 10) X(F_R2F16, 11) X(F_R2F16, 12)                                                             \
-    X(F_R2I16, 3) X(F_R2I16, 4) X(F_R2I16, 5) X(F_R2I16, 6) X(F_R2I16, 7) X(F_R2I16, 8) X(F_R2I16, 9)         \
-    X(F_R2I16, 10) X(F_R2I16, 11) X(F_R2I16, 12)                                                             \
-    X(F_R4F16, 4) X(F_R4F16, 6) X(F_R4F16, 8) X(F_R4F16, 10) X(F_R4F16, 12)                                   \
-    X(F_R8F16, 3) X(F_R8F16, 4) X(F_R8F16, 5) X(F_R8F16, 6) X(F_R8F16, 7) X(F_R8F16, 8) X(F_R8F16, 9)         \
-    X(F_R8F16, 10) X(F_R8F16, 11) X(F_R8F16, 12)
-#define GB_I32_VARIANTS(X)                                                                                   \
-    X(F_R2F32, 2) X(F_R2F32, 3) X(F_R2F32, 4) X(F_R2F32, 5) X(F_R2F32, 6) X(F_R2F32, 7) X(F_R2F32, 8)         \
-    X(F_R2F32, 9) X(F_R2F32, 10) X(F_R2F32, 11) X(F_R2F32, 12) X(F_R2F32, 13)                                \
-    X(F_R2G32, 2) X(F_R2G32, 3) X(F_R2G32, 4) X(F_R2G32, 5) X(F_R2G32, 6) X(F_R2G32, 7) X(F_R2G32, 8)         \
-    X(F_R2G32, 9) X(F_R2G32, 10) X(F_R2G32, 11) X(F_R2G32, 12) X(F_R2G32, 13)
-
-constexpr int SMEM_HEADER = 1024;   // mbarriers + the current segment's KArgs
-
-template <bool I32, int CTA, int ELMAX>
-__global__ void __launch_bounds__(CTA, (I32 || ELMAX > 5) ? 2 : 3) k_batch(const BatchDev b, int stage_bytes) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem);
-    KArgs* ka = reinterpret_cast<KArgs*>(smem + 64);
-    unsigned char* stage0 = smem + SMEM_HEADER;
-    int* xbuf = reinterpret_cast<int*>(smem + SMEM_HEADER + 2 * stage_bytes);
-    __shared__ long long sh_next;
-    __shared__ int sh_pending[2];
-    __shared__ int sh_failed;
-    const int tid = threadIdx.x;
-    const long long total = b.total_tiles;
-
-    auto seg_of = [&](long long t) {
-        int s = 0;
-        while (s + 1 < b.nsegs && __ldg(&b.segs[s + 1].tile0) <= t) ++s;
-        return s;
-    };
-    // thread 0: start the bulk load of tile t into buffer i
-    auto issue = [&](long long t, int i) {
-        const SegDev* sd = &b.segs[seg_of(t)];
-        const long long lt = t - sd->tile0;
-        const long long P = sd->polys_per_tile;
-        const long long count = sd->a.batch;
-        const long long np = min(P, count - lt * P);
-        const unsigned bytes = (unsigned)(np * sd->n * sd->elem_bytes);
-        const char* src = static_cast<const char*>(sd->a.in) + lt * P * sd->n * sd->elem_bytes;
-        mbar_expect_tx(&bar[i], bytes);
-        bulk_load(stage0 + i * stage_bytes, src, bytes, &bar[i]);
-    };
-
-    if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        const long long t0 = (long long)atomicAdd(&b.ctr[CTR_NEXT], 1ull);
-        sh_next = t0;
-        sh_pending[0] = 0;
-        sh_pending[1] = 0;
-        sh_failed = 0;
-        if (t0 < total) {
-            issue(t0, 0);
-            sh_pending[0] = 1;
-        }
-    }
-    __syncthreads();
-    long long t = sh_next;
-    unsigned phases = 0u;    // bit i: parity of the next completion of bar[i]
-    int buf = 0;
-    int cur_seg = -1;
-    KC kc;
-    while (t < total) {
-        const int s = seg_of(t);
-        const SegDev* sd = &b.segs[s];
-        if (tid == 0) {
-            const long long tn = (long long)atomicAdd(&b.ctr[CTR_NEXT], 1ull);
-            sh_next = tn;
-            if (tn < total) {
-                bulk_wait_read();           // the other buffer's last store has left shared memory
-                issue(tn, buf ^ 1);
-                sh_pending[buf ^ 1] = 1;
-            }
-        }
-        if (s != cur_seg) {
-            // every thread finished the previous tile (barrier at the loop end)
-            const int* src = reinterpret_cast<const int*>(&sd->a);
-            int* dst = reinterpret_cast<int*>(ka);
-            for (int w = tid; w < (int)(sizeof(KArgs) / 4); w += CTA) dst[w] = src[w];
-            cur_seg = s;
-            __syncthreads();
-            kc = make_kc(*ka);
-        }
-        if (!mbar_wait(&bar[buf], (phases >> buf) & 1u)) sh_failed = 1;
-        phases ^= 1u << buf;
-        const long long lt = t - sd->tile0;
-        const int P = sd->polys_per_tile;
-        const int np = (int)min((long long)P, sd->a.batch - lt * P);
-        const int variant = sd->variant;
-        void* st = stage0 + buf * stage_bytes;
-        switch (variant) {
-#define GB_CASE(F, L)                                                     \
-    case variant_id(F, L):                                                \
-        if constexpr (fam_i32(F) == I32) tile_transform<F, L, CTA, ELMAX>(st, xbuf, kc, np); \
-        break;
-            GB_I16_VARIANTS(GB_CASE)
-            GB_I32_VARIANTS(GB_CASE)
-#undef GB_CASE
-            default: break;
-        }
-        __syncthreads();
-        const long long tnext = sh_next;
-        if (sh_failed) break;
-        if (tid == 0) {
-            sh_pending[buf] = 0;
-            fence_proxy_async();
-            const long long off = lt * P * (long long)sd->n * sd->elem_bytes;
-            bulk_store(static_cast<char*>(sd->a.out) + off, st, (unsigned)(np * sd->n * sd->elem_bytes));
-            bulk_commit();
-        }
-        t = tnext;
-        buf ^= 1;
-    }
-    if (tid == 0) {
-        if (sh_failed) {
-            atomicMax(&b.ctr[CTR_ERROR], (unsigned long long)BERR_TIMEOUT);
-            // let a prefetch that is still in flight land before the CTA leaves (bounded)
-            // (bar[buf]'s parity bit was already advanced past the load it waited for)
-            for (int i = 0; i < 2; ++i)
-                if (sh_pending[i]) mbar_wait(&bar[i], ((phases >> i) & 1u) ^ (i == buf ? 1u : 0u));
-        }
-        bulk_wait_all();
-        __threadfence();
-        if (atomicAdd(&b.ctr[CTR_DONE], 1ull) == (unsigned long long)gridDim.x - 1) {
-            // last CTA of the launch: rearm the tile counter for the next launch
-            b.ctr[CTR_NEXT] = 0;
-            b.ctr[CTR_DONE] = 0;
-            __threadfence();
-        }
-    }
-}
-
-bool variant_supported(int fam, int L) {
-#define GB_HAS(F, L_) if (fam == F && L == L_) return true;
-    GB_I16_VARIANTS(GB_HAS)
-    GB_I32_VARIANTS(GB_HAS)
-#undef GB_HAS
-    return false;
-}
-
-constexpr int BATCH_CTA = 256;
-
-}  // namespace
-
-// persistent-kernel configurations: (storage type, coefficients per thread)
-struct BatchConfig {
-    bool i32;
-    int elmax;
-    const void* fn;
-};
-
-static const BatchConfig kConfigs[] = {
-    {false, 6, reinterpret_cast<const void*>(&k_batch<false, BATCH_CTA, 6>)},
-    {false, 5, reinterpret_cast<const void*>(&k_batch<false, BATCH_CTA, 5>)},
-    {true, 5, reinterpret_cast<const void*>(&k_batch<true, BATCH_CTA, 5>)},
-};
-
-}  // namespace gbntt
 
 using namespace gbntt;
 
 struct gbntt_batch {
     struct Layout {                     // one configuration of one persistent launch
-        int cfg = -1;                   // index into kConfigs
+        BatchConfig cfg{};
         std::vector<SegDev> segs;
         SegDev* d_segs = nullptr;
         long long total_tiles = 0;
         int stage_bytes = 0, smem = 0, grid = 0;
         float ms = -1.f;                // autotuner timing
     };
+    struct Pending {                    // a batched segment before the layouts are built
+        int k, fam, L, eb;
+        KArgs a;
+    };
     struct Part {                       // the int16 or the int32 segments
         bool i32 = false;
+        int fam_mask = 0;
+        std::vector<Pending> pending;
         std::vector<Layout> layouts;    // candidate configurations
         int chosen = 0;
         std::vector<int> user_index;    // caller's segment of each SegDev
@@ -216,7 +57,7 @@ int launch_layout(gbntt_batch* b, int pi, const gbntt_batch::Layout& lay, cudaSt
     bd.ctr = b->d_ctr + CTR_WORDS * pi;
     int sb = lay.stage_bytes;
     void* args[] = {&bd, &sb};
-    cudaError_t e = cudaLaunchKernel(kConfigs[lay.cfg].fn, dim3(lay.grid), dim3(BATCH_CTA), args, lay.smem, s);
+    cudaError_t e = cudaLaunchKernel(lay.cfg.fn, dim3(lay.grid), dim3(BATCH_CTA), args, lay.smem, s);
     if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
     gbntt_internal_count_launch();
     return GBNTT_OK;
@@ -306,19 +147,35 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
         if (id < 0) {
             id = b->nparts++;
             b->parts[id].i32 = i32;
-            for (int c = 0; c < (int)(sizeof(kConfigs) / sizeof(kConfigs[0])); ++c)
-                if (kConfigs[c].i32 == i32) {
-                    gbntt_batch::Layout lay;
-                    lay.cfg = c;
-                    b->parts[id].layouts.push_back(lay);
-                }
         }
         auto& part = b->parts[id];
         b->part_of[k] = id;
         b->index_in_part[k] = (int)part.user_index.size();
         part.user_index.push_back(k);
+        part.fam_mask |= 1 << fam;
+        part.pending.push_back({k, fam, L, eb, a});
+    }
+    // candidate configurations of each part: those whose family set covers it
+    for (int i = 0; i < b->nparts; ++i) {
+        auto& part = b->parts[i];
+        const BatchConfig* cfgs = nullptr;
+        const int ncfg = part.i32 ? batch_configs_i32(&cfgs) : batch_configs_i16(&cfgs);
+        for (int c = 0; c < ncfg; ++c)
+            if ((cfgs[c].set & part.fam_mask) == part.fam_mask) {
+                gbntt_batch::Layout lay;
+                lay.cfg = cfgs[c];
+                part.layouts.push_back(lay);
+            }
+        if (flags & GBNTT_BATCH_NO_TUNE) part.layouts.resize(1);   // the first (widest, most specific) one
+    }
+    for (int i = 0; i < b->nparts; ++i) {
+      auto& part = b->parts[i];
+      for (const auto& pe : part.pending) {
+        const gbntt_segment& u = segs[pe.k];
+        const int fam = pe.fam, L = pe.L, eb = pe.eb;
+        const KArgs& a = pe.a;
         for (auto& lay : part.layouts) {
-            const int elmax = kConfigs[lay.cfg].elmax;
+            const int elmax = lay.cfg.elmax;
             SegDev sd;
             std::memset(&sd, 0, sizeof(sd));
             sd.a = a;
@@ -337,6 +194,7 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
             lay.smem = std::max(lay.smem, batch_xbuf_bytes(BATCH_CTA, L, elmax));
             lay.segs.push_back(sd);
         }
+      }
     }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -345,7 +203,7 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
         for (auto& lay : b->parts[i].layouts) {
             lay.stage_bytes = (lay.stage_bytes + 127) & ~127;
             lay.smem = SMEM_HEADER + 2 * lay.stage_bytes + lay.smem;
-            const void* fn = kConfigs[lay.cfg].fn;
+            const void* fn = lay.cfg.fn;
             cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, lay.smem);
             int per_sm = 0;
             if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BATCH_CTA, lay.smem);
@@ -492,7 +350,8 @@ int gbntt_batch_query(const gbntt_batch* b, int what, int64_t* value) {
         case GBNTT_BQ_TILES: v += lay.total_tiles; break;
         case GBNTT_BQ_GRID: v = std::max<int64_t>(v, lay.grid); break;
         case GBNTT_BQ_SMEM: v = std::max<int64_t>(v, lay.smem); break;
-        case GBNTT_BQ_EL16: if (!b->parts[i].i32) v = kConfigs[lay.cfg].elmax; break;
+        case GBNTT_BQ_EL16: if (!b->parts[i].i32) v = lay.cfg.elmax; break;
+        case GBNTT_BQ_FAMSET: if (!b->parts[i].i32) v = lay.cfg.set; break;
         default: return batch_fail(GBNTT_ERR_ARG, "unknown query");
         }
     }

@@ -1,0 +1,26 @@
+// batch_k16.cu -- persistent-kernel instantiations for the int16 designs:
+// one per family (radix-2 forward + inverse, radix-4, radix-8) and a generic
+// one, each with 32 and 64 coefficients per thread.
+#include "batch_kernel.cuh"
+
+namespace gbntt {
+
+namespace {
+constexpr int R2 = (1 << F_R2F16) | (1 << F_R2I16);
+constexpr int R4 = 1 << F_R4F16;
+constexpr int R8 = 1 << F_R8F16;
+constexpr int ALL16 = R2 | R4 | R8;
+
+#define GB_CFG(EL, SET) {false, EL, SET, reinterpret_cast<const void*>(&k_batch<false, BATCH_CTA, EL, SET>)}
+const BatchConfig kI16[] = {
+    GB_CFG(6, R4), GB_CFG(5, R4), GB_CFG(6, R2), GB_CFG(5, R2), GB_CFG(6, R8), GB_CFG(5, R8), GB_CFG(5, ALL16),
+};
+#undef GB_CFG
+}  // namespace
+
+int batch_configs_i16(const BatchConfig** out) {
+    *out = kI16;
+    return (int)(sizeof(kI16) / sizeof(kI16[0]));
+}
+
+}  // namespace gbntt

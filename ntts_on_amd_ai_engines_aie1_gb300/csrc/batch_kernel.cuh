@@ -1,0 +1,171 @@
+// batch_kernel.cuh -- the persistent batch kernel template (instantiated in
+// batch_k16.cu and batch_k32.cu, launched by batch.cu).
+#pragma once
+
+#include "persist.cuh"
+
+namespace gbntt {
+
+constexpr int SMEM_HEADER = 1024;   // mbarriers + the current segment's KArgs
+constexpr int BATCH_CTA = 256;
+
+// every (family, L) the persistent kernels implement, per storage type
+#define GB_I16_VARIANTS(X)                                                                                   \
+    X(F_R2F16, 3) X(F_R2F16, 4) X(F_R2F16, 5) X(F_R2F16, 6) X(F_R2F16, 7) X(F_R2F16, 8) X(F_R2F16, 9)         \
+    X(F_R2F16, 10) X(F_R2F16, 11) X(F_R2F16, 12)                                                             \
+    X(F_R2I16, 3) X(F_R2I16, 4) X(F_R2I16, 5) X(F_R2I16, 6) X(F_R2I16, 7) X(F_R2I16, 8) X(F_R2I16, 9)         \
+    X(F_R2I16, 10) X(F_R2I16, 11) X(F_R2I16, 12)                                                             \
+    X(F_R4F16, 4) X(F_R4F16, 6) X(F_R4F16, 8) X(F_R4F16, 10) X(F_R4F16, 12)                                   \
+    X(F_R8F16, 3) X(F_R8F16, 4) X(F_R8F16, 5) X(F_R8F16, 6) X(F_R8F16, 7) X(F_R8F16, 8) X(F_R8F16, 9)         \
+    X(F_R8F16, 10) X(F_R8F16, 11) X(F_R8F16, 12)
+#define GB_I32_VARIANTS(X)                                                                                   \
+    X(F_R2F32, 2) X(F_R2F32, 3) X(F_R2F32, 4) X(F_R2F32, 5) X(F_R2F32, 6) X(F_R2F32, 7) X(F_R2F32, 8)         \
+    X(F_R2F32, 9) X(F_R2F32, 10) X(F_R2F32, 11) X(F_R2F32, 12) X(F_R2F32, 13)                                \
+    X(F_R2G32, 2) X(F_R2G32, 3) X(F_R2G32, 4) X(F_R2G32, 5) X(F_R2G32, 6) X(F_R2G32, 7) X(F_R2G32, 8)         \
+    X(F_R2G32, 9) X(F_R2G32, 10) X(F_R2G32, 11) X(F_R2G32, 12) X(F_R2G32, 13)
+
+// SET: bit mask of the families whose variants this instantiation carries
+// (one kernel per family keeps the register allocation of one design).
+template <bool I32, int CTA, int ELMAX, int SET>
+__global__ void __launch_bounds__(CTA, (I32 || ELMAX > 5) ? 2 : 3) k_batch(const BatchDev b, int stage_bytes) {
+    extern __shared__ __align__(128) unsigned char bsmem[];
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(bsmem);
+    KArgs* ka = reinterpret_cast<KArgs*>(bsmem + 64);
+    unsigned char* stage0 = bsmem + SMEM_HEADER;
+    int* xbuf = reinterpret_cast<int*>(bsmem + SMEM_HEADER + 2 * stage_bytes);
+    __shared__ long long sh_next;
+    __shared__ int sh_pending[2];
+    __shared__ int sh_failed;
+    const int tid = threadIdx.x;
+    const long long total = b.total_tiles;
+
+    auto seg_of = [&](long long t) {
+        int s = 0;
+        while (s + 1 < b.nsegs && __ldg(&b.segs[s + 1].tile0) <= t) ++s;
+        return s;
+    };
+    // thread 0: start the bulk load of tile t into buffer i
+    auto issue = [&](long long t, int i) {
+        const SegDev* sd = &b.segs[seg_of(t)];
+        const long long lt = t - sd->tile0;
+        const long long P = sd->polys_per_tile;
+        const long long count = sd->a.batch;
+        const long long np = min(P, count - lt * P);
+        const unsigned bytes = (unsigned)(np * sd->n * sd->elem_bytes);
+        const char* src = static_cast<const char*>(sd->a.in) + lt * P * sd->n * sd->elem_bytes;
+        mbar_expect_tx(&bar[i], bytes);
+        bulk_load(stage0 + i * stage_bytes, src, bytes, &bar[i]);
+    };
+
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        const long long t0 = (long long)atomicAdd(&b.ctr[CTR_NEXT], 1ull);
+        sh_next = t0;
+        sh_pending[0] = 0;
+        sh_pending[1] = 0;
+        sh_failed = 0;
+        if (t0 < total) {
+            issue(t0, 0);
+            sh_pending[0] = 1;
+        }
+    }
+    __syncthreads();
+    long long t = sh_next;
+    unsigned phases = 0u;    // bit i: parity of the next completion of bar[i]
+    int buf = 0;
+    int cur_seg = -1;
+    KC kc;
+    while (t < total) {
+        const int s = seg_of(t);
+        const SegDev* sd = &b.segs[s];
+        if (tid == 0) {
+            const long long tn = (long long)atomicAdd(&b.ctr[CTR_NEXT], 1ull);
+            sh_next = tn;
+            if (tn < total) {
+                bulk_wait_read();           // the other buffer's last store has left shared memory
+                issue(tn, buf ^ 1);
+                sh_pending[buf ^ 1] = 1;
+            }
+        }
+        if (s != cur_seg) {
+            // every thread finished the previous tile (barrier at the loop end)
+            const int* src = reinterpret_cast<const int*>(&sd->a);
+            int* dst = reinterpret_cast<int*>(ka);
+            for (int w = tid; w < (int)(sizeof(KArgs) / 4); w += CTA) dst[w] = src[w];
+            cur_seg = s;
+            __syncthreads();
+            kc = make_kc(*ka);
+        }
+        if (!mbar_wait(&bar[buf], (phases >> buf) & 1u)) sh_failed = 1;
+        phases ^= 1u << buf;
+        const long long lt = t - sd->tile0;
+        const int P = sd->polys_per_tile;
+        const int np = (int)min((long long)P, sd->a.batch - lt * P);
+        const int variant = sd->variant;
+        void* st = stage0 + buf * stage_bytes;
+        switch (variant) {
+#define GB_CASE(F, L)                                                     \
+    case variant_id(F, L):                                                \
+        if constexpr (fam_i32(F) == I32 && ((SET >> F) & 1)) tile_transform<F, L, CTA, ELMAX>(st, xbuf, kc, np); \
+        break;
+            GB_I16_VARIANTS(GB_CASE)
+            GB_I32_VARIANTS(GB_CASE)
+#undef GB_CASE
+            default: break;
+        }
+        __syncthreads();
+        const long long tnext = sh_next;
+        if (sh_failed) break;
+        if (tid == 0) {
+            sh_pending[buf] = 0;
+            fence_proxy_async();
+            const long long off = lt * P * (long long)sd->n * sd->elem_bytes;
+            bulk_store(static_cast<char*>(sd->a.out) + off, st, (unsigned)(np * sd->n * sd->elem_bytes));
+            bulk_commit();
+        }
+        t = tnext;
+        buf ^= 1;
+    }
+    if (tid == 0) {
+        if (sh_failed) {
+            atomicMax(&b.ctr[CTR_ERROR], (unsigned long long)BERR_TIMEOUT);
+            // let a prefetch that is still in flight land before the CTA leaves (bounded)
+            // (bar[buf]'s parity bit was already advanced past the load it waited for)
+            for (int i = 0; i < 2; ++i)
+                if (sh_pending[i]) mbar_wait(&bar[i], ((phases >> i) & 1u) ^ (i == buf ? 1u : 0u));
+        }
+        bulk_wait_all();
+        __threadfence();
+        if (atomicAdd(&b.ctr[CTR_DONE], 1ull) == (unsigned long long)gridDim.x - 1) {
+            // last CTA of the launch: rearm the tile counter for the next launch
+            b.ctr[CTR_NEXT] = 0;
+            b.ctr[CTR_DONE] = 0;
+            __threadfence();
+        }
+    }
+}
+
+inline bool variant_supported(int fam, int L) {
+#define GB_HAS(F, L_) if (fam == F && L == L_) return true;
+    GB_I16_VARIANTS(GB_HAS)
+    GB_I32_VARIANTS(GB_HAS)
+#undef GB_HAS
+    return false;
+}
+
+
+// one compiled configuration of the persistent kernel
+struct BatchConfig {
+    bool i32;
+    int elmax;   // log2 coefficients per thread
+    int set;     // families covered (bit F)
+    const void* fn;
+};
+
+// the configurations compiled into the library
+int batch_configs_i16(const BatchConfig** out);
+int batch_configs_i32(const BatchConfig** out);
+
+}  // namespace gbntt
