@@ -170,6 +170,26 @@ int gbntt_batch_status(gbntt_batch* batch);
 int gbntt_batch_query(const gbntt_batch* batch, int what, int64_t* value);
 int gbntt_batch_destroy(gbntt_batch* batch);
 
+/* ---- batch execution that allocates nothing ----
+ * No counterpart in the reference (its graphs own all their memory at compile
+ * time).  gbntt_batch_create allocates device memory for a batch's tile
+ * descriptors and counters; callers that cannot allocate device memory when
+ * they transform (an application that owns every device buffer through its own
+ * allocator or arena, a serving loop that must not synchronise the device with
+ * cudaMalloc/cudaFree in the middle of a request) use this call instead.  It
+ * runs the same persistent kernel on up to GBNTT_NOALLOC_MAX_SEGMENTS segments
+ * (plans created beforehand, caller-owned device buffers), keeping descriptors
+ * and counters in one fixed static device array (about 16 KB, held on every
+ * GPU that loads the library until the process exits).  More segments are
+ * rejected with GBNTT_ERR_ARG.  The first call on a device looks the array up
+ * (cudaGetSymbolAddress) with that device current; make that first call before
+ * any stream capture.  Every call reuses the array and resets its counters, so
+ * calls whose work overlaps on the GPU (different streams, no ordering
+ * between them) race; serialise them on one stream.  No autotuning: the
+ * configuration with 32 coefficients per thread is used. */
+#define GBNTT_NOALLOC_MAX_SEGMENTS 16
+int gbntt_batch_execute_noalloc(const gbntt_segment* segs, uint32_t nsegs, void* stream);
+
 /* Total number of kernels this library has launched in this process. */
 uint64_t gbntt_launch_count(void);
 
