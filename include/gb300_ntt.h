@@ -79,6 +79,10 @@ typedef enum gbntt_status {
 #define GBNTT_FLAG_R8_EXACT    0x2u  /* exact K=31 radix-8 multipliers (default for R8_I16_FWD)    */
 #define GBNTT_FLAG_R8_FLOAT    0x4u  /* the reference's float K=31 multipliers (src/twiddle.h:372;
                                         default for R8_I16_STAGE)                                  */
+#define GBNTT_FLAG_NATURAL_ORDER 0x8u /* bit-reversal unit fused into the transform: forward designs
+                                        return natural order, inverse designs take natural order   */
+#define GBNTT_FLAG_SCALE_NINV 0x10u  /* int16 inverse designs: the full Barrett unit multiplying by
+                                        n^-1 (src/project.cpp:154) fused into the store            */
 
 typedef struct gbntt_plan gbntt_plan;
 

@@ -41,6 +41,8 @@ class Kind(enum.IntEnum):
 FLAG_CANONICAL = 0x1
 FLAG_R8_EXACT = 0x2
 FLAG_R8_FLOAT = 0x4
+FLAG_NATURAL_ORDER = 0x8     # bit reversal fused: forward returns / inverse takes natural order
+FLAG_SCALE_NINV = 0x10       # int16 inverse: full Barrett multiplication by n^-1 fused
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported length", 3: "invalid modulus",
           4: "root of unity has the wrong order", 5: "radix-4 needs an even number of layers",

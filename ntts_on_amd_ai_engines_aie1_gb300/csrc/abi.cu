@@ -233,6 +233,12 @@ int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t
     a.fneg = hp.r4_fneg;
     a.wc = hp.r4_wc;
     a.canonical = (flags & FLAG_CANONICAL) ? 1 : 0;
+    const bool inverse = (kind == K_R2_I16_INV || kind == K_R2_I32_INV || kind == K_R4_I16_INV);
+    a.natural_in = ((flags & FLAG_NATURAL_ORDER) && inverse) ? 1 : 0;
+    a.natural_out = ((flags & FLAG_NATURAL_ORDER) && !inverse) ? 1 : 0;
+    a.scale = (flags & FLAG_SCALE_NINV) ? 1 : 0;
+    a.fb_fs = hp.fb_fs;
+    a.fb_wq = hp.fb_wq;
     a.r8_sym = hp.r8_sym;
     a.tail_wq = hp.tail_wq;
     for (int i = 0; i < 64; ++i) a.f8[i] = hp.f8[i];

@@ -38,6 +38,10 @@ struct KArgs {
     int c;                // Barrett constant of the reduction (K = 16 or 32)
     int fneg, wc;         // radix-4 omega_4 and its multiplier
     int canonical;        // reduce outputs to [0, q)
+    int natural_in;       // input in natural order (inverse designs): bit reversal fused into the load
+    int natural_out;      // output in natural order (forward designs): bit reversal fused into the store
+    int scale;            // inverse designs: full Barrett multiplication by n^-1 fused into the store
+    int fb_fs, fb_wq;     // its signed factor and multiplier
     int r8_sym;           // radix-8 matrix symmetric: use the factored butterfly
     int tail_wq;          // radix-8 tail stage multiplier of the twiddle 1
     int f8[64];           // radix-8 matrix [m][k]
@@ -53,6 +57,7 @@ struct KC {
     const int* f8;
     const int* ftail;
     int q, c, fneg, wc, canonical, r8_sym, tail_wq, f1, f2, f3, wq1;
+    int natural_in, natural_out, scale, fb_fs, fb_wq;
 };
 
 __device__ __forceinline__ KC make_kc(const KArgs& a) {
@@ -67,6 +72,11 @@ __device__ __forceinline__ KC make_kc(const KArgs& a) {
     k.fneg = a.fneg;
     k.wc = a.wc;
     k.canonical = a.canonical;
+    k.natural_in = a.natural_in;
+    k.natural_out = a.natural_out;
+    k.scale = a.scale;
+    k.fb_fs = a.fb_fs;
+    k.fb_wq = a.fb_wq;
     k.r8_sym = a.r8_sym;
     k.tail_wq = a.tail_wq;
     k.f1 = a.f8s[1];
@@ -123,10 +133,28 @@ __device__ __forceinline__ int r8red(int y, int tw, int wq, int q) {
     return wrap16((int)((unsigned)y * (unsigned)tw - (unsigned)m16 * (unsigned)q));
 }
 
+// Full Barrett multiplication by a constant, fully reduced
+// (src/kernels/full_reduction_kernels.cc:33-195).
+__device__ __forceinline__ int fb16(int x, int fs, int wq, int q) {
+    const int mb = wrap16(rsz16(x * wq));     // m' = SRS_16(x w'), symmetric_zero (:204-212)
+    const int r = x * fs - q * mb;            // x F_s - m' q (:234-238)
+    const int lo = wrap16(r);                 // low 16 bits (:241)
+    const int sign = wrap16(r >> 16);         // floor(r / 2^16) (:228, :242)
+    return wrap16(lo - sign * q);             // (:261-272)
+}
+
 // x mod q in [0, q)
 __device__ __forceinline__ int canon(int x, int q) {
     int r = x % q;
     return r < 0 ? r + q : r;
+}
+
+// the output epilogue shared by every kernel: fused n^-1 scaling, canonical form
+template <typename K>
+__device__ __forceinline__ int epilogue(int x, const K& a) {
+    if (a.scale) x = fb16(x, a.fb_fs, a.fb_wq, a.q);
+    if (a.canonical) x = canon(x, a.q);
+    return x;
 }
 
 // ---------------------------------------------------------------------------
@@ -415,13 +443,41 @@ __device__ __forceinline__ void run_steps(int (&v)[1 << EL], int* sp, int g, con
 // load / store of one polynomial in a window layout
 // ---------------------------------------------------------------------------
 
+template <bool I32, int L, int EL, int LO>
+__device__ __forceinline__ void load_poly_br(int (&v)[1 << EL], const KArgs& a, long long poly, int g) {
+    constexpr int E = 1 << EL;
+    constexpr long long N = 1LL << L;
+#pragma unroll
+    for (int k = 0; k < E; ++k) {
+        const int p = (int)(__brev((unsigned)posmap<LO, EL>(g, k)) >> (32 - L));
+        if constexpr (I32) v[k] = __ldg(static_cast<const int*>(a.in) + poly * N + p);
+        else v[k] = (int)__ldg(static_cast<const short*>(a.in) + poly * N + p);
+    }
+}
+
+template <bool I32, int L, int EL, int LO>
+__device__ __forceinline__ void store_poly_br(int (&v)[1 << EL], const KArgs& a, long long poly, int g) {
+    constexpr int E = 1 << EL;
+    constexpr long long N = 1LL << L;
+#pragma unroll
+    for (int k = 0; k < E; ++k) {
+        const int p = (int)(__brev((unsigned)posmap<LO, EL>(g, k)) >> (32 - L));
+        if constexpr (I32) static_cast<int*>(a.out)[poly * N + p] = v[k];
+        else static_cast<short*>(a.out)[poly * N + p] = (short)v[k];
+    }
+}
+
 template <bool I32, int L, int EL, int LO, bool BR>
 __device__ __forceinline__ void load_poly(int (&v)[1 << EL], const KArgs& a, long long poly, int g) {
     constexpr int E = 1 << EL;
     constexpr long long N = 1LL << L;
+    if (BR != (a.natural_in != 0)) {
+        load_poly_br<I32, L, EL, LO>(v, a, poly, g);
+        return;
+    }
     if constexpr (I32) {
         const int* src = static_cast<const int*>(a.in) + poly * N;
-        if constexpr (LO == 0 && !BR && E >= 4) {
+        if constexpr (LO == 0 && E >= 4) {
             const int4* s4 = reinterpret_cast<const int4*>(src + (long long)g * E);
 #pragma unroll
             for (int j = 0; j < E / 4; ++j) {
@@ -431,14 +487,12 @@ __device__ __forceinline__ void load_poly(int (&v)[1 << EL], const KArgs& a, lon
         } else {
 #pragma unroll
             for (int k = 0; k < E; ++k) {
-                int p = posmap<LO, EL>(g, k);
-                if constexpr (BR) p = (int)(__brev((unsigned)p) >> (32 - L));
-                v[k] = __ldg(src + p);
+                v[k] = __ldg(src + posmap<LO, EL>(g, k));
             }
         }
     } else {
         const short* src = static_cast<const short*>(a.in) + poly * N;
-        if constexpr (LO == 0 && !BR && E >= 8) {
+        if constexpr (LO == 0 && E >= 8) {
             const int4* s4 = reinterpret_cast<const int4*>(src + (long long)g * E);
 #pragma unroll
             for (int j = 0; j < E / 8; ++j) {
@@ -453,9 +507,7 @@ __device__ __forceinline__ void load_poly(int (&v)[1 << EL], const KArgs& a, lon
         } else {
 #pragma unroll
             for (int k = 0; k < E; ++k) {
-                int p = posmap<LO, EL>(g, k);
-                if constexpr (BR) p = (int)(__brev((unsigned)p) >> (32 - L));
-                v[k] = (int)__ldg(src + p);
+                v[k] = (int)__ldg(src + posmap<LO, EL>(g, k));
             }
         }
     }
@@ -465,27 +517,29 @@ template <bool I32, int L, int EL, int LO, bool BR>
 __device__ __forceinline__ void store_poly(int (&v)[1 << EL], const KArgs& a, long long poly, int g) {
     constexpr int E = 1 << EL;
     constexpr long long N = 1LL << L;
-    if (a.canonical) {
+    if (a.scale || a.canonical) {
 #pragma unroll
-        for (int k = 0; k < E; ++k) v[k] = canon(v[k], a.q);
+        for (int k = 0; k < E; ++k) v[k] = epilogue(v[k], a);
+    }
+    if (BR != (a.natural_out != 0)) {
+        store_poly_br<I32, L, EL, LO>(v, a, poly, g);
+        return;
     }
     if constexpr (I32) {
         int* dst = static_cast<int*>(a.out) + poly * N;
-        if constexpr (LO == 0 && !BR && E >= 4) {
+        if constexpr (LO == 0 && E >= 4) {
             int4* d4 = reinterpret_cast<int4*>(dst + (long long)g * E);
 #pragma unroll
             for (int j = 0; j < E / 4; ++j) d4[j] = make_int4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
         } else {
 #pragma unroll
             for (int k = 0; k < E; ++k) {
-                int p = posmap<LO, EL>(g, k);
-                if constexpr (BR) p = (int)(__brev((unsigned)p) >> (32 - L));
-                dst[p] = v[k];
+                dst[posmap<LO, EL>(g, k)] = v[k];
             }
         }
     } else {
         short* dst = static_cast<short*>(a.out) + poly * N;
-        if constexpr (LO == 0 && !BR && E >= 8) {
+        if constexpr (LO == 0 && E >= 8) {
             int4* d4 = reinterpret_cast<int4*>(dst + (long long)g * E);
 #pragma unroll
             for (int j = 0; j < E / 8; ++j) {
@@ -498,9 +552,7 @@ __device__ __forceinline__ void store_poly(int (&v)[1 << EL], const KArgs& a, lo
         } else {
 #pragma unroll
             for (int k = 0; k < E; ++k) {
-                int p = posmap<LO, EL>(g, k);
-                if constexpr (BR) p = (int)(__brev((unsigned)p) >> (32 - L));
-                dst[p] = (short)v[k];
+                dst[posmap<LO, EL>(g, k)] = (short)v[k];
             }
         }
     }

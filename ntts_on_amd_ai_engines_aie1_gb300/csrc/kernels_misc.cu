@@ -53,8 +53,7 @@ __global__ void __launch_bounds__(256) k_r8_stage(const KArgs a, int L) {
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             const int2 t = __ldg(&a.tab[k * M + i]);
-            int z = r8red(y[k], t.x, t.y, a.q);
-            if (a.canonical) z = canon(z, a.q);
+            const int z = epilogue(r8red(y[k], t.x, t.y, a.q), a);
             o[brev_c<3>(k)] = z;
         }
         int4 w;
@@ -90,16 +89,6 @@ __global__ void __launch_bounds__(256) k_bitrev(const KArgs a, int L, int P) {
         const int lp = j >> L, jj = j & (n - 1);
         dst[j] = sb[(lp << L) + (int)(__brev((unsigned)jj) >> (32 - L))];
     }
-}
-
-// Full Barrett multiplication by a constant, fully reduced
-// (src/kernels/full_reduction_kernels.cc:33-195).
-__device__ __forceinline__ int fb16(int x, int fs, int wq, int q) {
-    const int mb = wrap16(rsz16(x * wq));     // m' = SRS_16(x w'), symmetric_zero (:204-212)
-    const int r = x * fs - q * mb;            // x F_s - m' q (:234-238)
-    const int lo = wrap16(r);                 // low 16 bits (:241)
-    const int sign = wrap16(r >> 16);         // floor(r / 2^16) (:228, :242)
-    return wrap16(lo - sign * q);             // (:261-272)
 }
 
 __global__ void __launch_bounds__(256) k_full_barrett(const KArgs a, long long total, int fs, int wq) {

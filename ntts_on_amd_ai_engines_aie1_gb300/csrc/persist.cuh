@@ -124,14 +124,22 @@ __device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KC&
     int* sp = xbuf + lp * SW;
     int v[E];
     if (active) {
+        // natural-order input of an inverse design: the bit reversal is the read pattern
+        const unsigned br = a.natural_in ? 0xFFFFFFFFu : 0u;
         if constexpr (I32) {
             const int* s = static_cast<const int*>(stage) + lp * N;
 #pragma unroll
-            for (int k = 0; k < E; ++k) v[k] = s[posmap<LOS, EL>(g, k)];
+            for (int k = 0; k < E; ++k) {
+                const int p = posmap<LOS, EL>(g, k);
+                v[k] = s[br ? (int)(__brev((unsigned)p) >> (32 - L)) : p];
+            }
         } else {
             const short* s = static_cast<const short*>(stage) + lp * N;
 #pragma unroll
-            for (int k = 0; k < E; ++k) v[k] = s[posmap<LOS, EL>(g, k)];
+            for (int k = 0; k < E; ++k) {
+                const int p = posmap<LOS, EL>(g, k);
+                v[k] = s[br ? (int)(__brev((unsigned)p) >> (32 - L)) : p];
+            }
         }
     } else {
 #pragma unroll
@@ -139,11 +147,21 @@ __device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KC&
     }
     if constexpr (LO0 != LOS) exchange_windows<L, EL, LOS, LO0>(v, sp, g);
     run_steps<FAM, L, EL>(v, sp, g, a, std::make_integer_sequence<int, NS>{});
-    if (a.canonical) {
+    if (a.scale || a.canonical) {
 #pragma unroll
-        for (int k = 0; k < E; ++k) v[k] = canon(v[k], a.q);
+        for (int k = 0; k < E; ++k) v[k] = epilogue(v[k], a);
     }
     if (!active) return;
+    if (a.natural_out) {
+        // natural-order output of a forward design: bit-reversed scatter into the tile
+#pragma unroll
+        for (int k = 0; k < E; ++k) {
+            const int p = (int)(__brev((unsigned)posmap<LOZ, EL>(g, k)) >> (32 - L));
+            if constexpr (I32) static_cast<int*>(stage)[lp * N + p] = v[k];
+            else static_cast<short*>(stage)[lp * N + p] = (short)v[k];
+        }
+        return;
+    }
     if constexpr (LOZ == 0 && (I32 ? E >= 4 : E >= 8)) {
         // thread owns E consecutive coefficients: 16-byte stores
         if constexpr (I32) {

@@ -169,6 +169,17 @@ int build_host_plan(int kind, uint32_t n, int64_t q, int64_t root, int64_t facto
     }
     if (kind == K_FULL_BARRETT_I16 && (factor < 0 || factor >= q)) { err = "factor must lie in [0, q)"; return GBNTT_ERR_ARG; }
 
+    const bool inverse = (kind == K_R2_I16_INV || kind == K_R2_I32_INV || kind == K_R4_I16_INV);
+    const bool transform = (kind != K_BITREV_I16 && kind != K_FULL_BARRETT_I16 && kind != K_R8_I16_STAGE);
+    if ((flags & FLAG_NATURAL_ORDER) && !transform) {
+        err = "natural order applies to the transform designs only";
+        return GBNTT_ERR_ARG;
+    }
+    if ((flags & FLAG_SCALE_NINV) && !(kind == K_R2_I16_INV || kind == K_R4_I16_INV)) {
+        err = "the n^-1 epilogue applies to the int16 inverse designs only";
+        return GBNTT_ERR_ARG;
+    }
+    (void)inverse;
     hp.kind = kind; hp.n = n; hp.L = L < 0 ? 0 : L; hp.q = q; hp.root = root; hp.factor = factor;
     hp.flags = flags; hp.elem_bytes = is32 ? 4 : 2;
     if (kind != K_BITREV_I16) {
@@ -311,6 +322,15 @@ int build_host_plan(int kind, uint32_t n, int64_t q, int64_t root, int64_t facto
         hp.stages = 1;
         break;
     }
+    }
+    if (flags & FLAG_SCALE_NINV) {
+        // the FULL_BARRETT_MULTIPLICATION<n, q, n^-1> unit fused after the inverse
+        // (src/project.cpp:154, src/standalone_units.h:40)
+        const int64_t ninv = modinv(n, q);
+        const int64_t fs = ninv <= (q - 1) / 2 ? ninv : ninv - q;
+        hp.fb_fs = (int32_t)fs;
+        hp.fb_wq = fb_multiplier((int32_t)fs, (int32_t)q);
+        hp.stages += 1;
     }
     return GBNTT_OK;
 }

@@ -22,6 +22,8 @@ enum Kind {
 constexpr uint32_t FLAG_CANONICAL = 0x1u;
 constexpr uint32_t FLAG_R8_EXACT = 0x2u;
 constexpr uint32_t FLAG_R8_FLOAT = 0x4u;
+constexpr uint32_t FLAG_NATURAL_ORDER = 0x8u;
+constexpr uint32_t FLAG_SCALE_NINV = 0x10u;
 
 struct HostPlan {
     int kind = 0;

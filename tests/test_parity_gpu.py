@@ -236,3 +236,69 @@ def test_execute_host(gb, orc):
     st = gb.Plan(gb.Kind.R8_I16_STAGE, n, q, root_for(q, n))
     st.execute_host(x, out)
     assert np.array_equal(out, orc.Plan(orc.R8_I16_STAGE, n, q, root_for(q, n))(x))
+
+
+# ---------------------------------------------------------------------------
+# fused bit reversal (natural order) and fused n^-1 epilogue
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("kind,okind,q,n,dt,ok", [
+    (0, 0, 12289, 1024, np.int16, {}), (2, 2, 12289, 4096, np.int16, {}), (2, 2, 7681, 256, np.int16, {}),
+    (8, 8, 12289, 2048, np.int16, {"r8_exact": True}), (4, 4, 998244353, 4096, np.int32, {}),
+    (0, 0, 12289, 16, np.int16, {})])
+def test_natural_order_forward(gb, orc, kind, okind, q, n, dt, ok):
+    rng = np.random.default_rng(SEED + 1000 + n + kind)
+    x = inputs(rng, 13, n, 0, q, dt)
+    want = orc.Plan(okind, n, q, root_for(q, n), **ok)(x)[:, orc.bitrev_perm(n)]
+    got = gpu_run(gb, kind, n, q, root_for(q, n), x, flags=gb.FLAG_NATURAL_ORDER)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("kind,q,n,dt", [(1, 12289, 1024, np.int16), (1, 12289, 8, np.int16),
+                                         (9, 12289, 4096, np.int16), (5, 754974721, 2048, np.int32)])
+def test_natural_order_inverse_and_scale(gb, orc, kind, q, n, dt):
+    rng = np.random.default_rng(SEED + 1100 + n + kind)
+    x = inputs(rng, 7, n, -q, q, dt)
+    br = orc.bitrev_perm(n)
+    want = orc.Plan(kind, n, q, root_for(q, n))(np.ascontiguousarray(x[:, br]))
+    got = gpu_run(gb, kind, n, q, root_for(q, n), x, flags=gb.FLAG_NATURAL_ORDER)
+    assert np.array_equal(got, want)
+    if dt == np.int16:
+        fb = orc.Plan(orc.FULL_BARRETT_I16, n, q, 0, factor=pow(n, -1, q))
+        got = gpu_run(gb, kind, n, q, root_for(q, n), x, flags=gb.FLAG_SCALE_NINV)
+        assert np.array_equal(got, fb(orc.Plan(kind, n, q, root_for(q, n))(x)))
+
+
+def test_fused_roundtrip_returns_input(gb):
+    """natural-order forward, then natural-order inverse with the n^-1 epilogue: x back."""
+    q, n = 12289, 1024
+    x = np.random.default_rng(5).integers(0, q, (64, n)).astype(np.int16)
+    y = gpu_run(gb, 0, n, q, root_for(q, n), x, flags=gb.FLAG_NATURAL_ORDER)
+    z = gpu_run(gb, 1, n, q, root_for(q, n), y, flags=gb.FLAG_NATURAL_ORDER | gb.FLAG_SCALE_NINV)
+    assert np.array_equal(z.astype(np.int64) % q, x)
+    assert z.min() >= 0 and z.max() <= q
+
+
+def test_flags_in_a_batch(gb, orc):
+    q = 12289
+    rng = np.random.default_rng(77)
+    specs = [(2, 1024, gb.FLAG_NATURAL_ORDER), (1, 1024, gb.FLAG_SCALE_NINV),
+             (1, 256, gb.FLAG_NATURAL_ORDER | gb.FLAG_SCALE_NINV), (0, 512, gb.FLAG_NATURAL_ORDER)]
+    plans, xs, ys, wants = [], [], [], []
+    for kind, n, fl in specs:
+        x = rng.integers(0, q, (300, n)).astype(np.int16)
+        xin = np.ascontiguousarray(x[:, orc.bitrev_perm(n)]) if (fl & gb.FLAG_NATURAL_ORDER and kind == 1) else x
+        w = orc.Plan(kind, n, q, root_for(q, n))(xin)
+        if fl & gb.FLAG_SCALE_NINV:
+            w = orc.Plan(orc.FULL_BARRETT_I16, n, q, 0, factor=pow(n, -1, q))(w)
+        if fl & gb.FLAG_NATURAL_ORDER and kind != 1:
+            w = w[:, orc.bitrev_perm(n)]
+        plans.append(gb.Plan(kind, n, q, root_for(q, n), 0, fl))
+        xs.append(torch.from_numpy(x).cuda())
+        ys.append(torch.empty_like(xs[-1]))
+        wants.append(w)
+    b = gb.Batch(list(zip(plans, xs, ys)))
+    b.execute()
+    torch.cuda.synchronize()
+    for i, (y, w) in enumerate(zip(ys, wants)):
+        assert np.array_equal(y.cpu().numpy(), w), i
