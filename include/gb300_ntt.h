@@ -100,7 +100,9 @@ int gbntt_plan_destroy(gbntt_plan* plan);
 
 /* Transforms `batch` polynomials held in device memory, asynchronously on
  * `stream` (a cudaStream_t; NULL = legacy default stream).  One kernel launch
- * per call (two for R2_I32 with n > 8192). */
+ * per call, except the int32 designs with n >= 2^16 (up to 2^22), which run
+ * two passes (column and row sub-transforms) per chunk of at most 64 MiB of
+ * polynomials. */
 int gbntt_execute(const gbntt_plan* plan, const void* d_in, void* d_out, uint64_t batch,
                   void* stream);
 

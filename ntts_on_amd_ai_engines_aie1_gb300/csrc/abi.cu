@@ -1,4 +1,5 @@
 // abi.cu -- the C ABI of libgb300ntt.so (declared in include/gb300_ntt.h).
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -22,6 +23,7 @@ struct gbntt_plan {
     int fam = -1;          // transform family of k_ntt, -1 for the single-purpose kernels
     bool br = false;       // bit-reversed load and store (radix-4 inverse)
     KernelInfo ki;
+    LargeInfo large;       // int32 n >= 2^16: two-pass schedule (large.cols != nullptr)
     KArgs base;            // constants shared by every launch
     int2* d_tab = nullptr;
     size_t tab_bytes = 0;
@@ -77,7 +79,46 @@ int launch(const gbntt_plan* p, const void* d_in, void* d_out, uint64_t batch, c
     a.out = d_out;
     a.batch = (long long)batch;
     cudaError_t e = cudaSuccess;
-    if (p->fam >= 0) {
+    if (p->large.cols) {
+        // two passes per chunk of polynomials; a chunk (<= 64 MiB) stays in L2
+        // between its passes.  Forward: columns then rows; inverse: rows first.
+        const LargeInfo& li = p->large;
+        const long long n = (long long)p->hp.n;
+        long long chunk = (64LL << 20) / (n * 4);
+        if (chunk < 1) chunk = 1;
+        const bool inverse = (p->hp.kind == K_R2_I32_INV);
+        for (long long p0 = 0; p0 < (long long)batch; p0 += chunk) {
+            const long long np = std::min<long long>(chunk, (long long)batch - p0);
+            KArgs first = a, last = a;
+            first.in = static_cast<const int*>(d_in) + p0 * n;
+            first.out = static_cast<int*>(d_out) + p0 * n;
+            first.batch = np;
+            first.canonical = 0;    // the epilogue belongs to the last pass only
+            first.scale = 0;
+            last.in = first.out;
+            last.out = first.out;
+            last.batch = np;
+            int L1 = li.L1, L2 = li.L2;
+            void* cargs_first[] = {&first, &L2};
+            void* rargs_first[] = {&first, &L1};
+            void* cargs_last[] = {&last, &L2};
+            void* rargs_last[] = {&last, &L1};
+            const dim3 cgrid((unsigned)(np * ((1LL << li.L2) / li.cols_per_cta)));
+            const dim3 rgrid((unsigned)(((np << li.L1) + li.rows_per_cta - 1) / li.rows_per_cta));
+            if (!inverse) {
+                e = cudaLaunchKernel(li.cols, cgrid, dim3(li.cols_threads), cargs_first, li.cols_smem, s);
+                if (e == cudaSuccess)
+                    e = cudaLaunchKernel(li.rows, rgrid, dim3(li.rows_threads), rargs_last, li.rows_smem, s);
+            } else {
+                e = cudaLaunchKernel(li.rows, rgrid, dim3(li.rows_threads), rargs_first, li.rows_smem, s);
+                if (e == cudaSuccess)
+                    e = cudaLaunchKernel(li.cols, cgrid, dim3(li.cols_threads), cargs_last, li.cols_smem, s);
+            }
+            if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+            g_launches.fetch_add(2, std::memory_order_relaxed);
+        }
+        return GBNTT_OK;
+    } else if (p->fam >= 0) {
         const unsigned long long blocks = (batch + p->ki.polys - 1) / p->ki.polys;
         if (blocks > 0x7FFFFFFFull) return fail(GBNTT_ERR_ARG, "batch too large for one launch");
         void* args[] = {&a};
@@ -171,7 +212,13 @@ int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t
     const HostPlan& hp = p->hp;
     p->fam = family_of(kind);
     p->br = (kind == K_R4_I16_INV);
-    if (p->fam >= 0) {
+    if (p->fam >= 0 && hp.L >= 16) {
+        p->large = large_info(p->fam, hp.L);
+        if (!p->large.cols) {
+            delete p;
+            return fail(GBNTT_ERR_LENGTH, "no kernel for this length");
+        }
+    } else if (p->fam >= 0) {
         p->ki = kernel_for(p->fam, hp.L, p->br);
         if (!p->ki.fn) {
             delete p;
@@ -185,6 +232,15 @@ int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t
     }
     if (p->fam >= 0 && p->ki.smem > 48 * 1024) {
         e = cudaFuncSetAttribute(p->ki.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, p->ki.smem);
+        if (e != cudaSuccess) {
+            delete p;
+            return cuda_fail(e, "cudaFuncSetAttribute");
+        }
+    }
+    if (p->large.cols) {
+        e = cudaFuncSetAttribute(p->large.cols, cudaFuncAttributeMaxDynamicSharedMemorySize, p->large.cols_smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(p->large.rows, cudaFuncAttributeMaxDynamicSharedMemorySize, p->large.rows_smem);
         if (e != cudaSuccess) {
             delete p;
             return cuda_fail(e, "cudaFuncSetAttribute");

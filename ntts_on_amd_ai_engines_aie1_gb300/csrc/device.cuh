@@ -294,8 +294,24 @@ __host__ __device__ constexpr int brev_c(int x) {
 // butterflies of one step (all groups of the thread's window)
 // ---------------------------------------------------------------------------
 
-template <int FAM, int L, int EL, int S>
-__device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const KC& a) {
+// Column-interleaved exchange for the column pass of the two-pass schedule:
+// XC adjacent columns share the buffer, word = position * XC + column.
+template <int L, int EL, int LOA, int LOB, int XC>
+__device__ __forceinline__ void exchange_cols(int (&v)[1 << EL], int* sp, int g, int cl) {
+    constexpr int E = 1 << EL;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < E; ++k) sp[posmap<LOA, EL>(g, k) * XC + cl] = v[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < E; ++k) v[k] = sp[posmap<LOB, EL>(g, k) * XC + cl];
+}
+
+// XC > 0: column pass (XC columns per CTA, exchanges through exchange_cols);
+// HIB: row pass, the polynomial is row `hi` of a longer transform and the
+// twiddle block index carries hi in its top bits.
+template <int FAM, int L, int EL, int S, int XC = 0, bool HIB = false>
+__device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const KC& a, int hi = 0, int cl = 0) {
     constexpr int E = 1 << EL;
     constexpr int G = 1 << (L - EL);
     constexpr int LO = window_lo(FAM, L, EL, S);
@@ -305,7 +321,10 @@ __device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const
     static_assert(B >= LO && B + W <= LO + EL, "step outside its window");
     if constexpr (S > 0) {
         constexpr int PLO = window_lo(FAM, L, EL, S - 1);
-        if constexpr (PLO != LO) exchange_windows<L, EL, PLO, LO>(v, sp, g);
+        if constexpr (PLO != LO) {
+            if constexpr (XC > 0) exchange_cols<L, EL, PLO, LO, XC>(v, sp, g, cl);
+            else exchange_windows<L, EL, PLO, LO>(v, sp, g);
+        }
     }
     const int q = a.q;
 #pragma unroll
@@ -315,7 +334,7 @@ __device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const
             // forward CT layer S: block = position bits above B (src/kernels/
             // ntt_r2_kernels.cc:434-472, ntt_r2_int32_kernels.cc:267-295)
             const int k1 = k0 | (1 << KB);
-            const int blk = posmap<LO, EL>(g, k0) >> (B + 1);
+            const int blk = ((HIB ? (hi << L) : 0) | posmap<LO, EL>(g, k0)) >> (B + 1);
             if constexpr (FAM == F_R2F16) {
                 const int t = __ldg(&a.tab16[blk]);
                 const int u = br16(v[k0], a.c, q), w = bm16(v[k1], lo16(t), hi16(t), q);
@@ -330,7 +349,7 @@ __device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const
         } else if constexpr (FAM == F_R2G32) {
             // inverse GS layer S (ntt_r2_int32_kernels.cc:305-336)
             const int k1 = k0 | (1 << KB);
-            const int blk = posmap<LO, EL>(g, k0) >> (B + 1);
+            const int blk = ((HIB ? (hi << L) : 0) | posmap<LO, EL>(g, k0)) >> (B + 1);
             const int2 t = __ldg(&a.tab[blk]);
             const int s = add32(v[k0], v[k1]), d = sub32(v[k0], v[k1]);
             v[k0] = br32(s, a.c, q);
@@ -437,6 +456,12 @@ template <int FAM, int L, int EL, int... S>
 __device__ __forceinline__ void run_steps(int (&v)[1 << EL], int* sp, int g, const KC& a,
                                           std::integer_sequence<int, S...>) {
     (do_step<FAM, L, EL, S>(v, sp, g, a), ...);
+}
+
+template <int FAM, int L, int EL, int XC, bool HIB, int... S>
+__device__ __forceinline__ void run_steps_x(int (&v)[1 << EL], int* sp, int g, const KC& a, int hi, int cl,
+                                            std::integer_sequence<int, S...>) {
+    (do_step<FAM, L, EL, S, XC, HIB>(v, sp, g, a, hi, cl), ...);
 }
 
 // ---------------------------------------------------------------------------
@@ -633,6 +658,16 @@ KernelInfo kinfo_r2f32(int L);
 KernelInfo kinfo_r2g32(int L);
 KernelInfo kinfo_r4(int L, bool br);
 KernelInfo kinfo_r8(int L);
+
+// two-pass schedule for int32 transforms longer than one CTA holds (kernels_large.cu)
+struct LargeInfo {
+    const void* cols = nullptr;   // column pass kernel
+    const void* rows = nullptr;   // row pass kernel
+    int cols_threads = 0, cols_smem = 0, cols_per_cta = 0;
+    int rows_threads = 0, rows_smem = 0, rows_per_cta = 0;
+    int L1 = 0, L2 = 0;           // high (column-pass) and low (row-pass) index bits
+};
+LargeInfo large_info(int fam, int L);
 
 // single-purpose kernels (kernels_misc.cu)
 cudaError_t launch_r8_stage(const KArgs& a, int L, cudaStream_t s);

@@ -146,7 +146,7 @@ int build_host_plan(int kind, uint32_t n, int64_t q, int64_t root, int64_t facto
         err = "n must be a power of two >= 2 (src/auxiliary.h:11)";
         return GBNTT_ERR_LENGTH;
     }
-    const int max_L = is32 ? 15 : (kind == K_BITREV_I16 ? 16 : 12);
+    const int max_L = is32 ? 22 : (kind == K_BITREV_I16 ? 16 : 12);
     if (kind != K_FULL_BARRETT_I16 && L > max_L) { err = "n above the supported maximum for this design"; return GBNTT_ERR_LENGTH; }
     if (kind == K_R8_I16_STAGE && n < 16) { err = "the radix-8 stage needs n >= 16"; return GBNTT_ERR_LENGTH; }
     if (kind == K_R8_I16_FWD && n < 8) { err = "the radix-8 transform needs n >= 8"; return GBNTT_ERR_LENGTH; }
@@ -173,6 +173,10 @@ int build_host_plan(int kind, uint32_t n, int64_t q, int64_t root, int64_t facto
     const bool transform = (kind != K_BITREV_I16 && kind != K_FULL_BARRETT_I16 && kind != K_R8_I16_STAGE);
     if ((flags & FLAG_NATURAL_ORDER) && !transform) {
         err = "natural order applies to the transform designs only";
+        return GBNTT_ERR_ARG;
+    }
+    if ((flags & FLAG_NATURAL_ORDER) && is32 && L >= 16) {
+        err = "natural order is not available for the two-pass int32 lengths (n >= 2^16)";
         return GBNTT_ERR_ARG;
     }
     if ((flags & FLAG_SCALE_NINV) && !(kind == K_R2_I16_INV || kind == K_R4_I16_INV)) {

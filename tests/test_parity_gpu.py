@@ -302,3 +302,34 @@ def test_flags_in_a_batch(gb, orc):
     torch.cuda.synchronize()
     for i, (y, w) in enumerate(zip(ys, wants)):
         assert np.array_equal(y.cpu().numpy(), w), i
+
+
+@pytest.mark.parametrize("L", [16, 17, 19, 20])
+@pytest.mark.parametrize("q", [998244353, 754974721])
+def test_r2_i32_two_pass(gb, orc, q, L):
+    """n = 2^16 .. 2^20: column pass + row pass, bit-exact with the reference's layers."""
+    n = 1 << L
+    rng = np.random.default_rng(SEED + 1200 + L)
+    batch = 3 if L >= 19 else 5
+    root = root_for(q, n)
+    x = inputs(rng, batch, n, 0, q, np.int32)
+    y = check(gb, orc, gb.Kind.R2_I32_FWD, orc.R2_I32_FWD, n, q, root, x)
+    z = check(gb, orc, gb.Kind.R2_I32_INV, orc.R2_I32_INV, n, q, root, y)
+    assert np.array_equal(z.astype(np.int64) % q, x.astype(np.int64) * n % q)
+    got = gpu_run(gb, gb.Kind.R2_I32_FWD, n, q, root, x, flags=gb.FLAG_CANONICAL)
+    assert np.array_equal(got.astype(np.int64), y.astype(np.int64) % q)
+    got = gpu_run(gb, gb.Kind.R2_I32_INV, n, q, root, y, inplace=True)
+    assert np.array_equal(got, z)
+
+
+def test_r2_i32_two_pass_dft_column(gb, orc):
+    """n = 2^16 against the modular DFT at a few output positions."""
+    q, n = 469762049, 1 << 16
+    root = root_for(q, n)
+    x = np.random.default_rng(11).integers(0, q, n)
+    y = gpu_run(gb, gb.Kind.R2_I32_FWD, n, q, root, x.astype(np.int32)[None], flags=gb.FLAG_CANONICAL)[0]
+    br = n.bit_length() - 1
+    for k in (0, 1, 12345, n - 1):
+        want = sum(int(x[j]) * pow(root, j * k, q) for j in range(n)) % q
+        pos = int(format(k, f"0{br}b")[::-1], 2)
+        assert int(y[pos]) == want
