@@ -296,6 +296,10 @@ def run_ours(args):
                "d2h_bytes_per_step": algo_bytes // 2, "ms_per_step": e2e_ms, "steps": e2e_steps,
                "api": "gbntt_batch_execute_host (pinned host buffers, wall clock)"}
 
+    serving = None
+    if rank == 0 and not args.skip_serve:
+        serving = run_serving(gb, plans, inputs, args.serve_seconds)
+
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -325,11 +329,79 @@ def run_ours(args):
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": sampler.summary(t_wall0, t_wall1),
+        "serving": serving,
     }
     line.update(extra)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+SERVE_POLYS = 16          # polynomials per request (one plan per request)
+
+
+def run_serving(gb, plans, inputs, seconds):
+    """Continuous-batching server over the benchmark's three plans.
+
+    Requests of SERVE_POLYS polynomials pick a plan with the batch's weights
+    (1/4, 1/4, 1/2) and carry pinned host buffers.  First a saturating burst
+    measures the capacity (polynomials/s through host->device, kernel and
+    device->host); then open-loop Poisson arrivals at 50% and 90% of that
+    capacity give p50/p99 request latencies (submit to result in host memory)."""
+    import torch
+
+    rng = np.random.default_rng(SEED + 1)
+    ring = 512
+    h_in = [torch.from_numpy(np.ascontiguousarray(x[:SERVE_POLYS * 64])).pin_memory() for x in inputs]
+    h_out = [torch.empty((ring, SERVE_POLYS, x.shape[1]), dtype=torch.int16).pin_memory() for x in inputs]
+    srv = gb.Server(plans, slots=4)
+
+    def schedule(nreq, arrivals):
+        idx = rng.choice(3, size=nreq, p=[0.25, 0.25, 0.5]).tolist()
+        ins, outs = [], []
+        for k, i in enumerate(idx):
+            j = k % 64
+            ins.append(h_in[i][j * SERVE_POLYS:(j + 1) * SERVE_POLYS])
+            outs.append(h_out[i][k % ring])
+        return idx, ins, outs, [SERVE_POLYS] * nreq, arrivals
+
+    # correctness: a few requests against the direct launch of the same plan
+    idx, ins, outs, cnt, arr = schedule(48, [0.0] * 48)
+    tk = srv.submit_schedule(idx, ins, outs, cnt, arr)
+    for t in tk:
+        srv.wait(t)
+    for i, a, b in zip(idx, ins, outs):
+        assert torch.equal(plans[i](a.cuda()).cpu(), b), "served result differs from the direct launch"
+
+    def run(nreq, arrivals):
+        srv.stats(reset=True)
+        idx, ins, outs, cnt, arr = schedule(nreq, arrivals)
+        t0 = time.perf_counter()
+        srv.submit_schedule(idx, ins, outs, cnt, arr)
+        srv.drain()
+        el = time.perf_counter() - t0
+        st = srv.stats()
+        assert st["completed"] == nreq and st["refused"] == 0
+        return st, el
+
+    run(2000, [0.0] * 2000)                                       # warm-up
+    nsat = 20000
+    st, el = run(nsat, [0.0] * nsat)
+    cap = nsat * SERVE_POLYS / el
+    out = {"request_polys": SERVE_POLYS, "slots": 4, "api": "gbntt_server_* (pinned host buffers)",
+           "saturation": {"polys_per_s": cap, "requests": nsat, "microbatches": st["microbatches"],
+                          "p50_us": st["p50_us"], "p99_us": st["p99_us"]}}
+    for frac in (0.5, 0.9):
+        rate = frac * cap / SERVE_POLYS                             # requests per second
+        nreq = max(200, int(rate * seconds))
+        arrivals = np.cumsum(rng.exponential(1e6 / rate, nreq)).tolist()
+        st, el = run(nreq, arrivals)
+        out[f"poisson_{int(frac * 100)}"] = {
+            "offered_polys_per_s": rate * SERVE_POLYS, "achieved_polys_per_s": nreq * SERVE_POLYS / el,
+            "requests": nreq, "p50_us": st["p50_us"], "p99_us": st["p99_us"], "max_us": st["max_us"],
+            "microbatches": st["microbatches"], "peak_arena_bytes": st["peak_arena_bytes"]}
+    srv.close()
+    return out
 
 
 PROFILE_CASES = {
@@ -340,6 +412,9 @@ PROFILE_CASES = {
     "r2f32_4096": (4, 4096, 998244353, 63912897, 16384),
     "r2g32_4096": (5, 4096, 998244353, 63912897, 16384),
     "r8_4096": (8, 4096, 12289, 41, 16384),
+    "r2f32_1m": (4, 1 << 20, 998244353, 565042129, 64),
+    "r2g32_1m": (5, 1 << 20, 998244353, 565042129, 64),
+    "r2f32_16k": (4, 1 << 14, 998244353, 666702199, 4096),
     "batch_r4": None,   # the benchmark batch, 4x larger, persistent kernel
 }
 
@@ -409,6 +484,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-per-ntt", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-serve", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=1.5)
     ap.add_argument("--profile", choices=sorted(PROFILE_CASES), default=None,
                     help="run one design on a large batch (for ncu captures) instead of the benchmark")
     args = ap.parse_args()

@@ -196,6 +196,44 @@ int gbntt_batch_destroy(gbntt_batch* batch);
 #define GBNTT_NOALLOC_MAX_SEGMENTS 16
 int gbntt_batch_execute_noalloc(const gbntt_segment* segs, uint32_t nsegs, void* stream);
 
+/* ---- serving loop: continuous batching of transform requests ----
+ * Requests (a plan of the server, host input, host output, polynomial count)
+ * may be submitted from any host thread.  A worker thread admits them while
+ * the server's device arena has room (its size is the configured budget,
+ * capped at half of the HBM free at creation), groups the waiting ones by
+ * plan into a micro-batch per free stream slot (one in-place launch per plan
+ * group), and overlaps the copies and kernels of up to `slots` micro-batches.
+ * Host buffers should be pinned for the copies to overlap.  Requests larger
+ * than the whole arena are refused (their wait returns GBNTT_ERR_ADMISSION).
+ * Latency = submit to completion as seen by the worker. */
+typedef struct gbntt_server gbntt_server;
+typedef struct gbntt_server_config {
+    uint32_t slots;                   /* concurrent micro-batches (streams); 0 = 4 */
+    uint32_t max_requests_per_batch;  /* 0 = 4096                                  */
+    uint64_t device_bytes;            /* arena budget; 0 = 1 GiB                   */
+} gbntt_server_config;
+typedef struct gbntt_server_stats {
+    uint64_t completed, refused, polynomials, microbatches, launches;
+    double p50_us, p99_us, max_us;    /* request latency percentiles (nearest rank) */
+    double polys_per_s;               /* polynomials completed per second           */
+    uint64_t arena_bytes, peak_arena_bytes;
+} gbntt_server_stats;
+int gbntt_server_create(gbntt_server** server, const gbntt_plan* const* plans, uint32_t nplans,
+                        const gbntt_server_config* cfg);
+int gbntt_server_submit(gbntt_server* server, uint32_t plan, const void* h_in, void* h_out, uint64_t count,
+                        uint64_t* ticket);
+int gbntt_server_wait(gbntt_server* server, uint64_t ticket, uint32_t timeout_ms);
+int gbntt_server_drain(gbntt_server* server, uint32_t timeout_ms);
+int gbntt_server_get_stats(gbntt_server* server, gbntt_server_stats* stats, int reset);
+int gbntt_server_destroy(gbntt_server* server);
+/* Open-loop load generator: submits request i at arrival_us[i] microseconds
+ * after the call (busy-waiting), writing its ticket to tickets[i]. */
+int gbntt_server_submit_schedule(gbntt_server* server, uint64_t nreq, const uint32_t* plan,
+                                 const void* const* h_in, void* const* h_out, const uint64_t* count,
+                                 const double* arrival_us, uint64_t* tickets);
+/* Checks the arena allocator and the percentile code on the host (no CUDA). */
+int gbntt_server_selftest(void);
+
 /* Total number of kernels this library has launched in this process. */
 uint64_t gbntt_launch_count(void);
 

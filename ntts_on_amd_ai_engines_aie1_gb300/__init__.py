@@ -62,6 +62,18 @@ class Segment(ctypes.Structure):
                 ("count", ctypes.c_uint64)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("slots", ctypes.c_uint32), ("max_requests_per_batch", ctypes.c_uint32),
+                ("device_bytes", ctypes.c_uint64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_uint64), ("refused", ctypes.c_uint64), ("polynomials", ctypes.c_uint64),
+                ("microbatches", ctypes.c_uint64), ("launches", ctypes.c_uint64), ("p50_us", ctypes.c_double),
+                ("p99_us", ctypes.c_double), ("max_us", ctypes.c_double), ("polys_per_s", ctypes.c_double),
+                ("arena_bytes", ctypes.c_uint64), ("peak_arena_bytes", ctypes.c_uint64)]
+
+
 _lib = None
 
 
@@ -89,6 +101,15 @@ def lib():
         L.gbntt_batch_status.argtypes = [vp]
         L.gbntt_batch_query.argtypes = [vp, i32, ctypes.POINTER(i64)]
         L.gbntt_batch_destroy.argtypes = [vp]
+        L.gbntt_server_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(vp), u32, ctypes.POINTER(ServerConfig)]
+        L.gbntt_server_submit.argtypes = [vp, u32, vp, vp, u64, ctypes.POINTER(u64)]
+        L.gbntt_server_wait.argtypes = [vp, u64, u32]
+        L.gbntt_server_drain.argtypes = [vp, u32]
+        L.gbntt_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats), i32]
+        L.gbntt_server_destroy.argtypes = [vp]
+        L.gbntt_server_submit_schedule.argtypes = [vp, u64, ctypes.POINTER(u32), ctypes.POINTER(vp),
+                                                   ctypes.POINTER(vp), ctypes.POINTER(u64),
+                                                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(u64)]
         L.gbntt_launch_count.restype = u64
         L.gbntt_last_error.restype = ctypes.c_char_p
         L.gbntt_status_string.restype = ctypes.c_char_p
@@ -254,6 +275,66 @@ class Batch:
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
             lib().gbntt_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _hptr(a):
+    return a.ctypes.data if hasattr(a, "ctypes") else a.data_ptr()
+
+
+class Server:
+    """Continuous-batching request server over a fixed list of plans."""
+
+    def __init__(self, plans, slots=4, device_bytes=0, max_requests_per_batch=0):
+        self.plans = list(plans)
+        arr = (ctypes.c_void_p * len(self.plans))(*[p.handle for p in self.plans])
+        cfg = ServerConfig(slots, max_requests_per_batch, device_bytes)
+        h = ctypes.c_void_p()
+        _check(lib().gbntt_server_create(ctypes.byref(h), arr, len(self.plans), ctypes.byref(cfg)))
+        self._h = h
+
+    def submit(self, plan, h_in, h_out, count=None):
+        t = ctypes.c_uint64(0)
+        cnt = count if count is not None else (h_in.size if hasattr(h_in, "ctypes") else h_in.numel()) \
+            // self.plans[plan].n
+        _check(lib().gbntt_server_submit(self._h, plan, _hptr(h_in), _hptr(h_out), cnt, ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket, timeout_ms=60000):
+        """0 when done; raises NTTError (timeout, refused) otherwise."""
+        _check(lib().gbntt_server_wait(self._h, ticket, timeout_ms))
+
+    def try_wait(self, ticket, timeout_ms=60000):
+        return lib().gbntt_server_wait(self._h, ticket, timeout_ms)
+
+    def drain(self, timeout_ms=600000):
+        _check(lib().gbntt_server_drain(self._h, timeout_ms))
+
+    def submit_schedule(self, plan_idx, h_ins, h_outs, counts, arrival_us):
+        n = len(plan_idx)
+        P = (ctypes.c_uint32 * n)(*plan_idx)
+        I = (ctypes.c_void_p * n)(*[_hptr(a) for a in h_ins])
+        O = (ctypes.c_void_p * n)(*[_hptr(a) for a in h_outs])
+        C = (ctypes.c_uint64 * n)(*counts)
+        A = (ctypes.c_double * n)(*arrival_us)
+        T = (ctypes.c_uint64 * n)()
+        _check(lib().gbntt_server_submit_schedule(self._h, n, P, I, O, C, A, T))
+        return list(T)
+
+    def stats(self, reset=False):
+        st = ServerStats()
+        _check(lib().gbntt_server_get_stats(self._h, ctypes.byref(st), int(reset)))
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().gbntt_server_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

@@ -1,0 +1,488 @@
+// serve.cu -- the serving loop (gbntt_server_* in include/gb300_ntt.h).
+//
+// Requests (plan, host input, host output, polynomial count) arrive from any
+// host thread.  One worker thread runs continuous batching:
+//   * admission: a request is admitted when the device arena (sized from the
+//     free HBM at start-up) has room for its polynomials; requests larger than
+//     the whole arena are refused;
+//   * micro-batches: the admitted requests that are waiting when a stream
+//     slot is free are grouped by plan; each plan group gets one contiguous
+//     arena block, its inputs are copied in, one in-place launch transforms
+//     the group, the outputs are copied back, and an event closes the slot;
+//   * while slots are busy on the GPU, newly arrived requests are admitted
+//     into the next micro-batch, so copies and kernels of different
+//     micro-batches overlap on the device;
+//   * completion is observed by polling the slots' events; latencies (submit
+//     to completion) feed the p50/p99 statistics.
+// All waits on the host are bounded by the caller's timeout.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/gb300_ntt.h"
+#include "plan_internal.h"
+
+namespace gbntt {
+
+// First-fit allocator over one device arena, in units of ALIGN bytes.  Host
+// bookkeeping only (no CUDA calls), so it is tested without a GPU.
+class Arena {
+public:
+    static constexpr size_t ALIGN = 256;
+    explicit Arena(size_t bytes = 0) { reset(bytes); }
+    void reset(size_t bytes) {
+        cap_ = bytes / ALIGN * ALIGN;
+        free_.clear();
+        if (cap_) free_[0] = cap_;
+        used_ = 0;
+    }
+    // offset of a block of `bytes`, or SIZE_MAX when it does not fit now
+    size_t alloc(size_t bytes) {
+        const size_t need = (bytes + ALIGN - 1) / ALIGN * ALIGN;
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= need) {
+                const size_t off = it->first, len = it->second;
+                free_.erase(it);
+                if (len > need) free_[off + need] = len - need;
+                used_ += need;
+                return off;
+            }
+        }
+        return SIZE_MAX;
+    }
+    void release(size_t off, size_t bytes) {
+        const size_t need = (bytes + ALIGN - 1) / ALIGN * ALIGN;
+        used_ -= need;
+        auto it = free_.emplace(off, need).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {   // merge with the next block
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {                                        // and with the previous one
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    size_t capacity() const { return cap_; }
+    size_t used() const { return used_; }
+    size_t largest_free() const {
+        size_t m = 0;
+        for (const auto& f : free_) m = std::max(m, f.second);
+        return m;
+    }
+
+private:
+    size_t cap_ = 0, used_ = 0;
+    std::map<size_t, size_t> free_;   // offset -> length
+};
+
+// p-th percentile (0..100) by nearest rank of an unsorted sample
+double percentile(std::vector<double> v, double p) {
+    if (v.empty()) return 0.0;
+    std::sort(v.begin(), v.end());
+    size_t rank = (size_t)std::ceil(p / 100.0 * (double)v.size());
+    if (rank < 1) rank = 1;
+    if (rank > v.size()) rank = v.size();
+    return v[rank - 1];
+}
+
+}  // namespace gbntt
+
+using namespace gbntt;
+using Clock = std::chrono::steady_clock;
+
+namespace {
+
+struct Request {
+    uint64_t ticket;
+    uint32_t plan;
+    const void* h_in;
+    void* h_out;
+    uint64_t count;
+    size_t bytes;
+    Clock::time_point t_submit;
+};
+
+struct Group {                  // one plan's requests in one micro-batch
+    uint32_t plan;
+    size_t off = 0, bytes = 0;
+    uint64_t count = 0;
+    std::vector<Request> reqs;
+};
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    bool busy = false;
+    std::vector<Group> groups;
+};
+
+}  // namespace
+
+struct gbntt_server {
+    std::vector<const gbntt_plan*> plans;
+    std::vector<int64_t> plan_bytes;   // bytes of one polynomial
+    std::vector<Slot> slots;
+    Arena arena;
+    char* d_arena = nullptr;
+    uint32_t max_group_requests = 0;
+    int device = 0;
+
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Request> pending;
+    std::unordered_map<uint64_t, int> status;   // ticket -> status (absent: in flight)
+    uint64_t next_ticket = 1;
+    bool stop = false;
+    std::thread worker;
+    int worker_error = GBNTT_OK;
+    std::string worker_msg;
+
+    // statistics (guarded by mu)
+    std::vector<double> lat_us;
+    uint64_t completed = 0, refused = 0, polys = 0, microbatches = 0, launches = 0;
+    size_t peak_used = 0;
+    Clock::time_point t_first, t_last;
+};
+
+namespace {
+
+int sfail(int code, const std::string& m) { return gbntt_internal_fail(code, m); }
+
+void finish_slot(gbntt_server* s, Slot& sl) {
+    const auto now = Clock::now();
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (auto& g : sl.groups) {
+        s->arena.release(g.off, g.bytes);
+        for (auto& r : g.reqs) {
+            s->status[r.ticket] = GBNTT_OK;
+            s->lat_us.push_back(std::chrono::duration<double, std::micro>(now - r.t_submit).count());
+            s->polys += r.count;
+            ++s->completed;
+        }
+    }
+    s->t_last = now;
+    sl.groups.clear();
+    sl.busy = false;
+    s->cv_done.notify_all();
+    s->cv_work.notify_all();
+}
+
+// Issue one micro-batch on slot sl (copies in, one launch per plan group, copies out).
+int issue(gbntt_server* s, Slot& sl) {
+    for (auto& g : sl.groups) {
+        char* base = s->d_arena + g.off;
+        size_t at = 0;
+        for (auto& r : g.reqs) {
+            cudaError_t e = cudaMemcpyAsync(base + at, r.h_in, r.bytes, cudaMemcpyHostToDevice, sl.stream);
+            if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve H2D: ") + cudaGetErrorString(e));
+            at += r.bytes;
+        }
+        const int rc = gbntt_execute(s->plans[g.plan], base, base, g.count, sl.stream);
+        if (rc != GBNTT_OK) return rc;
+        ++s->launches;
+        at = 0;
+        for (auto& r : g.reqs) {
+            cudaError_t e = cudaMemcpyAsync(r.h_out, base + at, r.bytes, cudaMemcpyDeviceToHost, sl.stream);
+            if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve D2H: ") + cudaGetErrorString(e));
+            at += r.bytes;
+        }
+    }
+    cudaError_t e = cudaEventRecord(sl.done, sl.stream);
+    if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve event: ") + cudaGetErrorString(e));
+    sl.busy = true;
+    ++s->microbatches;
+    return GBNTT_OK;
+}
+
+void worker_main(gbntt_server* s) {
+    cudaSetDevice(s->device);
+    for (;;) {
+        // 1. completions
+        bool any_busy = false;
+        for (auto& sl : s->slots) {
+            if (!sl.busy) continue;
+            const cudaError_t q = cudaEventQuery(sl.done);
+            if (q == cudaSuccess) finish_slot(s, sl);
+            else if (q == cudaErrorNotReady) any_busy = true;
+            else {
+                std::lock_guard<std::mutex> lk(s->mu);
+                s->worker_error = GBNTT_ERR_CUDA;
+                s->worker_msg = std::string("serve: ") + cudaGetErrorString(q);
+                s->stop = true;
+            }
+        }
+        // 2. admission into a free slot
+        Slot* free_slot = nullptr;
+        for (auto& sl : s->slots)
+            if (!sl.busy) { free_slot = &sl; break; }
+        std::vector<Group> groups;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            if (s->stop && (s->pending.empty() || s->worker_error)) {
+                if (!any_busy) break;
+            }
+            if (free_slot && !s->pending.empty()) {
+                // take waiting requests in arrival order while the arena has room
+                std::map<uint32_t, size_t> gi;
+                uint32_t taken = 0;
+                size_t mb_bytes = 0;
+                const size_t budget = s->arena.capacity() / s->slots.size();   // one slot's share
+                while (!s->pending.empty() && taken < s->max_group_requests) {
+                    Request& r = s->pending.front();
+                    if (taken && mb_bytes + r.bytes > budget) break;
+                    mb_bytes += r.bytes;
+                    auto it = gi.find(r.plan);
+                    Group* g;
+                    if (it == gi.end()) {
+                        gi[r.plan] = groups.size();
+                        groups.push_back(Group());
+                        g = &groups.back();
+                        g->plan = r.plan;
+                    } else {
+                        g = &groups[it->second];
+                    }
+                    g->reqs.push_back(r);
+                    g->count += r.count;
+                    g->bytes += r.bytes;
+                    s->pending.pop_front();
+                    ++taken;
+                }
+                // reserve one arena block per group; what does not fit goes back to the queue front
+                for (size_t i = groups.size(); i-- > 0;) {
+                    Group& g = groups[i];
+                    g.off = s->arena.alloc(g.bytes);
+                    if (g.off == SIZE_MAX) {
+                        for (auto r = g.reqs.rbegin(); r != g.reqs.rend(); ++r) s->pending.push_front(*r);
+                        groups.erase(groups.begin() + (long)i);
+                    }
+                }
+                s->peak_used = std::max(s->peak_used, s->arena.used());
+            } else if (!any_busy && s->pending.empty() && !s->stop) {
+                s->cv_work.wait_for(lk, std::chrono::milliseconds(2));
+                continue;
+            }
+        }
+        if (!groups.empty()) {
+            free_slot->groups = std::move(groups);
+            const int rc = issue(s, *free_slot);
+            if (rc != GBNTT_OK) {
+                std::lock_guard<std::mutex> lk(s->mu);
+                s->worker_error = rc;
+                s->worker_msg = gbntt_last_error();
+                s->stop = true;
+            }
+        } else if (any_busy) {
+            std::this_thread::yield();
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbntt_server_create(gbntt_server** out, const gbntt_plan* const* plans, uint32_t nplans,
+                        const gbntt_server_config* cfg) {
+    if (!out || !plans || !nplans) return sfail(GBNTT_ERR_ARG, "server needs at least one plan");
+    *out = nullptr;
+    gbntt_server* s = new gbntt_server();
+    s->plans.assign(plans, plans + nplans);
+    for (auto* p : s->plans) {
+        int64_t n = 0, eb = 0;
+        if (!p || gbntt_plan_query(p, GBNTT_Q_N, &n) || gbntt_plan_query(p, GBNTT_Q_ELEM_BYTES, &eb)) {
+            delete s;
+            return sfail(GBNTT_ERR_ARG, "invalid plan");
+        }
+        int64_t kind = 0;
+        gbntt_plan_query(p, GBNTT_Q_KIND, &kind);
+        if (kind == GBNTT_R8_I16_STAGE) {
+            delete s;
+            return sfail(GBNTT_ERR_ARG, "the radix-8 stage cannot run in place and is not served");
+        }
+        s->plan_bytes.push_back(n * eb);
+    }
+    const uint32_t nslots = cfg && cfg->slots ? cfg->slots : 4;
+    s->max_group_requests = cfg && cfg->max_requests_per_batch ? cfg->max_requests_per_batch : 4096;
+    cudaGetDevice(&s->device);
+    size_t free_b = 0, total_b = 0;
+    cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
+    if (e != cudaSuccess) {
+        delete s;
+        return sfail(GBNTT_ERR_CUDA, std::string("cudaMemGetInfo: ") + cudaGetErrorString(e));
+    }
+    // admission budget: the configured bytes, capped at half of the free HBM
+    size_t want = cfg && cfg->device_bytes ? (size_t)cfg->device_bytes : (size_t)1 << 30;
+    want = std::min(want, free_b / 2);
+    s->arena.reset(want);
+    if (s->arena.capacity() == 0) {
+        delete s;
+        return sfail(GBNTT_ERR_ADMISSION, "no device memory for the request arena");
+    }
+    e = cudaMalloc(&s->d_arena, s->arena.capacity());
+    if (e != cudaSuccess) {
+        delete s;
+        return sfail(GBNTT_ERR_NOMEM, "request arena allocation failed");
+    }
+    s->slots.resize(nslots);
+    for (auto& sl : s->slots) {
+        cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+        cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+    }
+    s->t_first = s->t_last = Clock::now();
+    s->worker = std::thread(worker_main, s);
+    *out = s;
+    return GBNTT_OK;
+}
+
+int gbntt_server_submit(gbntt_server* s, uint32_t plan, const void* h_in, void* h_out, uint64_t count,
+                        uint64_t* ticket) {
+    if (!s || !ticket) return sfail(GBNTT_ERR_ARG, "null argument");
+    if (plan >= s->plans.size()) return sfail(GBNTT_ERR_ARG, "plan index out of range");
+    if (!h_in || !h_out || !count) return sfail(GBNTT_ERR_ARG, "request without data");
+    const size_t bytes = (size_t)count * (size_t)s->plan_bytes[plan];
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->worker_error) return sfail(s->worker_error, s->worker_msg);
+    const uint64_t t = s->next_ticket++;
+    *ticket = t;
+    if ((bytes + Arena::ALIGN - 1) / Arena::ALIGN * Arena::ALIGN > s->arena.capacity()) {
+        s->status[t] = GBNTT_ERR_ADMISSION;   // can never fit: refused, not queued
+        ++s->refused;
+        s->cv_done.notify_all();
+        return GBNTT_OK;
+    }
+    if (s->completed == 0 && s->pending.empty() && s->microbatches == 0) s->t_first = Clock::now();
+    s->pending.push_back(Request{t, plan, h_in, h_out, count, bytes, Clock::now()});
+    s->cv_work.notify_one();
+    return GBNTT_OK;
+}
+
+int gbntt_server_wait(gbntt_server* s, uint64_t ticket, uint32_t timeout_ms) {
+    if (!s) return sfail(GBNTT_ERR_ARG, "server is null");
+    std::unique_lock<std::mutex> lk(s->mu);
+    const auto deadline = Clock::now() + std::chrono::milliseconds(timeout_ms);
+    for (;;) {
+        auto it = s->status.find(ticket);
+        if (it != s->status.end()) {
+            const int st = it->second;
+            s->status.erase(it);
+            return st == GBNTT_OK ? GBNTT_OK : sfail(st, "request refused: larger than the admission budget");
+        }
+        if (s->worker_error) return sfail(s->worker_error, s->worker_msg);
+        if (s->cv_done.wait_until(lk, deadline) == std::cv_status::timeout) {
+            if (s->status.count(ticket)) continue;
+            return sfail(GBNTT_ERR_TIMEOUT, "request not finished within the timeout");
+        }
+    }
+}
+
+int gbntt_server_drain(gbntt_server* s, uint32_t timeout_ms) {
+    if (!s) return sfail(GBNTT_ERR_ARG, "server is null");
+    std::unique_lock<std::mutex> lk(s->mu);
+    const auto deadline = Clock::now() + std::chrono::milliseconds(timeout_ms);
+    for (;;) {
+        bool busy = !s->pending.empty();
+        for (auto& sl : s->slots) busy = busy || sl.busy;
+        if (!busy) return GBNTT_OK;
+        if (s->worker_error) return sfail(s->worker_error, s->worker_msg);
+        if (s->cv_done.wait_until(lk, deadline) == std::cv_status::timeout)
+            return sfail(GBNTT_ERR_TIMEOUT, "server did not drain within the timeout");
+    }
+}
+
+int gbntt_server_get_stats(gbntt_server* s, gbntt_server_stats* st, int reset) {
+    if (!s || !st) return sfail(GBNTT_ERR_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    std::memset(st, 0, sizeof(*st));
+    st->completed = s->completed;
+    st->refused = s->refused;
+    st->polynomials = s->polys;
+    st->microbatches = s->microbatches;
+    st->launches = s->launches;
+    st->p50_us = percentile(s->lat_us, 50.0);
+    st->p99_us = percentile(s->lat_us, 99.0);
+    st->max_us = s->lat_us.empty() ? 0.0 : *std::max_element(s->lat_us.begin(), s->lat_us.end());
+    const double secs = std::chrono::duration<double>(s->t_last - s->t_first).count();
+    st->polys_per_s = secs > 0 ? (double)s->polys / secs : 0.0;
+    st->arena_bytes = s->arena.capacity();
+    st->peak_arena_bytes = s->peak_used;
+    if (reset) {
+        s->lat_us.clear();
+        s->completed = s->refused = s->polys = s->microbatches = s->launches = 0;
+        s->peak_used = 0;
+        s->t_first = s->t_last = Clock::now();
+    }
+    return GBNTT_OK;
+}
+
+int gbntt_server_destroy(gbntt_server* s) {
+    if (!s) return GBNTT_OK;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+        s->cv_work.notify_all();
+    }
+    if (s->worker.joinable()) s->worker.join();
+    for (auto& sl : s->slots) {
+        if (sl.stream) cudaStreamSynchronize(sl.stream);
+        if (sl.done) cudaEventDestroy(sl.done);
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+    }
+    if (s->d_arena) cudaFree(s->d_arena);
+    delete s;
+    return GBNTT_OK;
+}
+
+// Open-loop load generator: submits request i at arrival_us[i] microseconds
+// after the call (busy-waiting between arrivals), from the calling thread.
+int gbntt_server_submit_schedule(gbntt_server* s, uint64_t nreq, const uint32_t* plan,
+                                 const void* const* h_in, void* const* h_out, const uint64_t* count,
+                                 const double* arrival_us, uint64_t* tickets) {
+    if (!s || (nreq && (!plan || !h_in || !h_out || !count || !arrival_us || !tickets)))
+        return sfail(GBNTT_ERR_ARG, "null argument");
+    const auto t0 = Clock::now();
+    for (uint64_t i = 0; i < nreq; ++i) {
+        const auto due = t0 + std::chrono::nanoseconds((long long)(arrival_us[i] * 1000.0));
+        while (Clock::now() < due) {
+        }
+        const int rc = gbntt_server_submit(s, plan[i], h_in[i], h_out[i], count[i], &tickets[i]);
+        if (rc != GBNTT_OK) return rc;
+    }
+    return GBNTT_OK;
+}
+
+// Host-side self test of the admission arena and the percentile code (no CUDA).
+int gbntt_server_selftest(void) {
+    Arena a(4096);
+    const size_t x = a.alloc(1000), y = a.alloc(1000), z = a.alloc(1000);
+    if (x != 0 || y != 1024 || z != 2048 || a.used() != 3072) return sfail(GBNTT_ERR_ARG, "arena: first fit");
+    if (a.alloc(2000) != SIZE_MAX) return sfail(GBNTT_ERR_ARG, "arena: over-admission");
+    a.release(y, 1000);
+    if (a.alloc(1024) != 1024) return sfail(GBNTT_ERR_ARG, "arena: reuse");
+    a.release(x, 1000);
+    a.release(1024, 1024);
+    a.release(z, 1000);
+    if (a.used() != 0 || a.largest_free() != 4096) return sfail(GBNTT_ERR_ARG, "arena: coalescing");
+    std::vector<double> v;
+    for (int i = 1; i <= 100; ++i) v.push_back(101 - i);
+    if (percentile(v, 50) != 50 || percentile(v, 99) != 99 || percentile(v, 100) != 100)
+        return sfail(GBNTT_ERR_ARG, "percentile");
+    return GBNTT_OK;
+}
+
+}  // extern "C"

@@ -139,3 +139,8 @@ def test_full_barrett_constants(gb, orc):
     c = gb.host_tables(gb.Kind.FULL_BARRETT_I16, 4096, 12289, 0, 12286, which=1)
     o = orc.Plan(orc.FULL_BARRETT_I16, 4096, 12289, 0, factor=12286).table(5)
     assert c[3] == o[4] and c[4] == o[5]
+
+
+def test_server_host_logic(gb):
+    """Admission arena (first fit, coalescing, no over-admission) and percentiles."""
+    assert gb.lib().gbntt_server_selftest() == 0, gb.lib().gbntt_last_error()
