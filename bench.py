@@ -277,7 +277,7 @@ def run_ours(args):
 
     e2e = None
     if not args.skip_e2e:
-        # end to end through the C ABI: pinned host buffers, H2D + one launch + D2H per step
+        # end to end through the C ABI: pinned host buffers in, results in host memory out
         h_in = [torch.from_numpy(x).pin_memory() for x in inputs]
         h_out = [torch.empty_like(x).pin_memory() for x in h_in]
         e2e_steps = max(3, min(args.steps, 100))
@@ -294,11 +294,16 @@ def run_ours(args):
             assert np.array_equal(h_out[i][:128].numpy(), want)
         e2e = {"value": polys / (e2e_ms / 1e3), "unit": "NTT/s", "h2d_bytes_per_step": algo_bytes // 2,
                "d2h_bytes_per_step": algo_bytes // 2, "ms_per_step": e2e_ms, "steps": e2e_steps,
-               "api": "gbntt_batch_execute_host (pinned host buffers, wall clock)"}
+               "api": "gbntt_batch_execute_host, wall clock; pinned host buffers, which the zero-copy persistent "
+                      "kernel reads and writes directly over the host-device link (one launch per step)"}
+
+    configs = None
+    if rank == 0 and not args.skip_configs:
+        configs = run_configs(gb, oracle, flush, stream, peak)
 
     serving = None
     if rank == 0 and not args.skip_serve:
-        serving = run_serving(gb, plans, inputs, args.serve_seconds)
+        serving = run_serving(gb, args.serve_seconds)
 
     if rank != 0:
         if dist:
@@ -330,6 +335,7 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": sampler.summary(t_wall0, t_wall1),
         "serving": serving,
+        "other_configs": configs,
     }
     line.update(extra)
     print(json.dumps(line), flush=True)
@@ -337,69 +343,215 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-SERVE_POLYS = 16          # polynomials per request (one plan per request)
+def run_configs(gb, oracle, flush, stream, peak):
+    """The other workloads, measured beside the headline (device-resident
+    inputs, L2 flushed before each timed launch, CUDA events on the stream):
+    C1 radix-2 int16 forward then inverse, n = 1024, one polynomial (latency);
+    C2 radix-2 int32 forward + inverse, n = 4096, 1024 polynomials for each of
+    four primes; C4a ragged radix-8 int16 forward with the bit reversal fused
+    (natural-order output), 2000 polynomials of n = 2^U, U uniform in {8..12},
+    one persistent launch; C4b radix-2 int32 forward and inverse of 64
+    polynomials of n = 2^20 (two-pass schedule).  Each is checked against the
+    oracle on a sample first."""
+    import torch
+
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(SEED + 2)
+    out = {}
+
+    def timed(fn, steps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for _ in range(3):
+            fn()
+        for a, b in evs:
+            flush.zero_()
+            a.record(stream)
+            fn()
+            b.record(stream)
+        torch.cuda.synchronize()
+        return statistics.median([a.elapsed_time(b) for a, b in evs])
+
+    # C1
+    q, n = 12289, 1024
+    root = pow(41, 4, q)
+    f = gb.Plan(gb.Kind.R2_I16_FWD, n, q, root)
+    i = gb.Plan(gb.Kind.R2_I16_INV, n, q, root)
+    x = rng.integers(0, q, (1, n)).astype(np.int16)
+    dx = torch.from_numpy(x).to(dev)
+    y = torch.empty_like(dx)
+    z = torch.empty_like(dx)
+    f.execute(dx, y, 1, stream)
+    i.execute(y, z, 1, stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(y.cpu().numpy(), oracle.Plan(oracle.R2_I16_FWD, n, q, root)(x))
+    assert np.array_equal(z.cpu().numpy() % q, (x.astype(np.int64) * n) % q)
+    ms = timed(lambda: (f.execute(dx, y, 1, stream), i.execute(y, z, 1, stream)), 200)
+    out["C1_r2_i16_fwd_inv_n1024"] = {"us_per_fwd_inv_pair": ms * 1e3, "launches": 2}
+
+    # C2
+    n, cnt = 4096, 1024
+    tot_ms, ok = 0.0, True
+    for qq, g in SERVE_Q32:
+        root = pow(g, (qq - 1) // n, qq)
+        f = gb.Plan(gb.Kind.R2_I32_FWD, n, qq, root)
+        i = gb.Plan(gb.Kind.R2_I32_INV, n, qq, root)
+        x = rng.integers(0, qq, (cnt, n)).astype(np.int32)
+        dx = torch.from_numpy(x).to(dev)
+        y = torch.empty_like(dx)
+        z = torch.empty_like(dx)
+        f.execute(dx, y, cnt, stream)
+        i.execute(y, z, cnt, stream)
+        torch.cuda.synchronize()
+        ok &= np.array_equal(y[:4].cpu().numpy(), oracle.Plan(oracle.R2_I32_FWD, n, qq, root)(x[:4]))
+        ok &= np.array_equal(z[:4].cpu().numpy().astype(np.int64) % qq, (x[:4].astype(np.int64) * n) % qq)
+        tot_ms += timed(lambda: (f.execute(dx, y, cnt, stream), i.execute(y, z, cnt, stream)), 50)
+    assert ok, "C2 differs from the oracle"
+    b = 4 * 2 * cnt * 2 * n * 4
+    out["C2_r2_i32_fwd_inv_n4096_4primes"] = {"NTT_per_s": 4 * 2 * cnt / (tot_ms / 1e3), "GBps": b / (tot_ms / 1e3) / 1e9,
+                                             "frac_of_hbm": b / (tot_ms / 1e3) / 1e9 / peak, "ms": tot_ms}
+
+    # C4a
+    q = 12289
+    U = rng.integers(8, 13, 2000)
+    segs, keep, algo = [], [], 0
+    for L in range(8, 13):
+        c = int((U == L).sum())
+        n = 1 << L
+        p = gb.Plan(gb.Kind.R8_I16_FWD, n, q, pow(41, 4096 // n, q), flags=gb.FLAG_NATURAL_ORDER)
+        x = rng.integers(0, q, (c, n)).astype(np.int16)
+        dx = torch.from_numpy(x).to(dev)
+        dy = torch.empty_like(dx)
+        segs.append((p, dx, dy))
+        keep.append((x, dy, n))
+        algo += 2 * 2 * n * c
+    batch = gb.Batch(segs)
+    batch.execute(stream)
+    torch.cuda.synchronize()
+    for x, dy, n in keep:
+        want = oracle.Plan(oracle.R8_I16_FWD, n, q, pow(41, 4096 // n, q), r8_exact=True)(x[:8])[:, oracle.bitrev_perm(n)]
+        assert np.array_equal(dy[:8].cpu().numpy(), want), "C4a differs from the oracle"
+    ms = timed(lambda: batch.graph_launch(stream), 200)
+    out["C4a_ragged_r8_i16_natural_2000"] = {"NTT_per_s": 2000 / (ms / 1e3), "GBps": algo / (ms / 1e3) / 1e9,
+                                            "frac_of_hbm": algo / (ms / 1e3) / 1e9 / peak, "us": ms * 1e3,
+                                            "launches": batch.query(0)}
+
+    # C4b
+    q, n, cnt = 998244353, 1 << 20, 64
+    root = 565042129
+    f = gb.Plan(gb.Kind.R2_I32_FWD, n, q, root)
+    i = gb.Plan(gb.Kind.R2_I32_INV, n, q, root)
+    x = rng.integers(0, q, (cnt, n)).astype(np.int32)
+    dx = torch.from_numpy(x).to(dev)
+    y = torch.empty_like(dx)
+    z = torch.empty_like(dx)
+    f.execute(dx, y, cnt, stream)
+    i.execute(y, z, cnt, stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(y[:1].cpu().numpy(), oracle.Plan(oracle.R2_I32_FWD, n, q, root)(x[:1]))
+    assert np.array_equal(z[:2].cpu().numpy().astype(np.int64) % q, (x[:2].astype(np.int64) * n) % q)
+    b = 2 * n * 4 * cnt
+    for name, pl, src, dst in (("fwd", f, dx, y), ("inv", i, y, z)):
+        ms = timed(lambda: pl.execute(src, dst, cnt, stream), 20)
+        out[f"C4b_r2_i32_{name}_n2^20_64"] = {"NTT_per_s": cnt / (ms / 1e3), "GBps": b / (ms / 1e3) / 1e9,
+                                             "frac_of_hbm": b / (ms / 1e3) / 1e9 / peak, "ms": ms}
+    return out
 
 
-def run_serving(gb, plans, inputs, seconds):
-    """Continuous-batching server over the benchmark's three plans.
+SERVE_Q32 = [(998244353, 3), (469762049, 3), (167772161, 3), (754974721, 11)]   # (q, generator)
 
-    Requests of SERVE_POLYS polynomials pick a plan with the batch's weights
-    (1/4, 1/4, 1/2) and carry pinned host buffers.  First a saturating burst
-    measures the capacity (polynomials/s through host->device, kernel and
-    device->host); then open-loop Poisson arrivals at 50% and 90% of that
-    capacity give p50/p99 request latencies (submit to result in host memory)."""
+
+def run_serving(gb, seconds):
+    """Serving loop over a stream of single-polynomial requests.
+
+    n = 2^U with U uniform in {8..16}, forward/inverse 50/50, int16 (q = 12289)
+    or int32 (four NTT primes) 50/50.  q = 12289 has no root of unity of order
+    above 4096 and no int16-storable prime below the lazy-reduction bound has
+    one of order 8192, so int16 requests draw U again from {8..12}.  Host
+    buffers are pinned.  A saturating burst measures the capacity; open-loop
+    Poisson arrivals at 50% and 90% of it give p50/p99 latency (submit to
+    result in host memory).  A sample of requests is checked against the same
+    transform launched alone."""
     import torch
 
     rng = np.random.default_rng(SEED + 1)
-    ring = 512
-    h_in = [torch.from_numpy(np.ascontiguousarray(x[:SERVE_POLYS * 64])).pin_memory() for x in inputs]
-    h_out = [torch.empty((ring, SERVE_POLYS, x.shape[1]), dtype=torch.int16).pin_memory() for x in inputs]
+    plans, keys = [], {}
+    for inv in (0, 1):
+        for L in range(8, 13):
+            n = 1 << L
+            keys[(16, 12289, L, inv)] = len(plans)
+            plans.append(gb.Plan(gb.Kind.R2_I16_INV if inv else gb.Kind.R2_I16_FWD, n, 12289, pow(41, 4096 // n, 12289)))
+        for q, g in SERVE_Q32:
+            for L in range(8, 17):
+                n = 1 << L
+                keys[(32, q, L, inv)] = len(plans)
+                plans.append(gb.Plan(gb.Kind.R2_I32_INV if inv else gb.Kind.R2_I32_FWD, n, q, pow(g, (q - 1) // n, q)))
+    pool = {}      # (dtype bits, q, L) -> pinned input polynomials
+    for (bits, q, L, inv) in keys:
+        if (bits, q, L) not in pool:
+            dt = np.int16 if bits == 16 else np.int32
+            pool[(bits, q, L)] = torch.from_numpy(rng.integers(0, q, (4, 1 << L)).astype(dt)).pin_memory()
+    ring = 8
+    outs = {k: torch.empty((ring,) + v.shape[1:], dtype=v.dtype).pin_memory() for k, v in pool.items()}
+
+    def draw(nreq):
+        bits = rng.integers(0, 2, nreq)
+        U = rng.integers(8, 17, nreq)
+        U16 = rng.integers(8, 13, nreq)
+        inv = rng.integers(0, 2, nreq)
+        qi = rng.integers(0, len(SERVE_Q32), nreq)
+        idx, ins, outl, nbytes = [], [], [], 0
+        for k in range(nreq):
+            if bits[k] == 0:
+                key = (16, 12289, int(U16[k]))
+            else:
+                key = (32, SERVE_Q32[qi[k]][0], int(U[k]))
+            idx.append(keys[key + (int(inv[k]),)])
+            ins.append(pool[key][k % 4])
+            outl.append(outs[key][k % ring])
+            nbytes += 2 * (1 << key[2]) * (key[0] // 8)
+        return idx, ins, outl, nbytes
+
     srv = gb.Server(plans, slots=4)
-
-    def schedule(nreq, arrivals):
-        idx = rng.choice(3, size=nreq, p=[0.25, 0.25, 0.5]).tolist()
-        ins, outs = [], []
-        for k, i in enumerate(idx):
-            j = k % 64
-            ins.append(h_in[i][j * SERVE_POLYS:(j + 1) * SERVE_POLYS])
-            outs.append(h_out[i][k % ring])
-        return idx, ins, outs, [SERVE_POLYS] * nreq, arrivals
-
-    # correctness: a few requests against the direct launch of the same plan
-    idx, ins, outs, cnt, arr = schedule(48, [0.0] * 48)
-    tk = srv.submit_schedule(idx, ins, outs, cnt, arr)
-    for t in tk:
+    # alone-vs-mix: a mixed burst with distinct output buffers, each checked against a lone launch
+    idx, ins, _, _ = draw(256)
+    own = [torch.empty_like(x).pin_memory() for x in ins]
+    for t in srv.submit_schedule(idx, ins, own, [1] * len(idx), [0.0] * len(idx)):
         srv.wait(t)
-    for i, a, b in zip(idx, ins, outs):
-        assert torch.equal(plans[i](a.cuda()).cpu(), b), "served result differs from the direct launch"
+    for i, x, y in zip(idx, ins, own):
+        assert torch.equal(plans[i](x.unsqueeze(0).cuda()).cpu()[0], y), "served result differs from a lone launch"
 
     def run(nreq, arrivals):
         srv.stats(reset=True)
-        idx, ins, outs, cnt, arr = schedule(nreq, arrivals)
+        idx, ins, outl, nbytes = draw(nreq)
         t0 = time.perf_counter()
-        srv.submit_schedule(idx, ins, outs, cnt, arr)
+        srv.submit_schedule(idx, ins, outl, [1] * nreq, arrivals)
         srv.drain()
         el = time.perf_counter() - t0
         st = srv.stats()
         assert st["completed"] == nreq and st["refused"] == 0
-        return st, el
+        return st, el, nbytes
 
-    run(2000, [0.0] * 2000)                                       # warm-up
-    nsat = 20000
-    st, el = run(nsat, [0.0] * nsat)
-    cap = nsat * SERVE_POLYS / el
-    out = {"request_polys": SERVE_POLYS, "slots": 4, "api": "gbntt_server_* (pinned host buffers)",
-           "saturation": {"polys_per_s": cap, "requests": nsat, "microbatches": st["microbatches"],
+    run(5000, [0.0] * 5000)                                         # warm-up
+    nsat = 50000
+    st, el, nbytes = run(nsat, [0.0] * nsat)
+    cap = nsat / el
+    out = {"workload": "single-polynomial requests: n=2^U, U~{8..16} (int16: {8..12}), fwd/inv 50/50, "
+                       "int16 q=12289 / int32 q in {998244353,469762049,167772161,754974721} 50/50",
+           "plans": len(plans), "slots": 4, "api": "gbntt_server_* (pinned host buffers)",
+           "alone_vs_mix_checked": 256,
+           "saturation": {"requests_per_s": cap, "NTT_per_s": cap, "algorithmic_GBps": nbytes / el / 1e9,
+                          "requests": nsat, "microbatches": st["microbatches"], "launches": st["launches"],
                           "p50_us": st["p50_us"], "p99_us": st["p99_us"]}}
     for frac in (0.5, 0.9):
-        rate = frac * cap / SERVE_POLYS                             # requests per second
-        nreq = max(200, int(rate * seconds))
+        rate = frac * cap
+        nreq = int(min(200000, max(1000, rate * seconds)))
         arrivals = np.cumsum(rng.exponential(1e6 / rate, nreq)).tolist()
-        st, el = run(nreq, arrivals)
+        st, el, nbytes = run(nreq, arrivals)
         out[f"poisson_{int(frac * 100)}"] = {
-            "offered_polys_per_s": rate * SERVE_POLYS, "achieved_polys_per_s": nreq * SERVE_POLYS / el,
-            "requests": nreq, "p50_us": st["p50_us"], "p99_us": st["p99_us"], "max_us": st["max_us"],
-            "microbatches": st["microbatches"], "peak_arena_bytes": st["peak_arena_bytes"]}
+            "offered_requests_per_s": rate, "achieved_requests_per_s": nreq / el, "requests": nreq,
+            "p50_us": st["p50_us"], "p99_us": st["p99_us"], "max_us": st["max_us"],
+            "microbatches": st["microbatches"], "launches": st["launches"],
+            "peak_arena_bytes": st["peak_arena_bytes"]}
     srv.close()
     return out
 
@@ -485,6 +637,7 @@ def main():
     ap.add_argument("--skip-per-ntt", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-serve", action="store_true")
+    ap.add_argument("--skip-configs", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=1.5)
     ap.add_argument("--profile", choices=sorted(PROFILE_CASES), default=None,
                     help="run one design on a large batch (for ncu captures) instead of the benchmark")

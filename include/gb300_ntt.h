@@ -158,9 +158,16 @@ int gbntt_batch_create(gbntt_batch** batch, const gbntt_segment* segs, uint32_t 
 int gbntt_batch_execute(gbntt_batch* batch, void* stream);
 /* The same launches captured once in a CUDA graph and replayed. */
 int gbntt_batch_graph_launch(gbntt_batch* batch, void* stream);
-/* Host buffers: copies h_in[i] into segment i's device input, runs the batch
- * (graph replay), copies every segment's device output to h_out[i] and waits
- * for the stream.  Pinned host buffers give full copy bandwidth. */
+/* Host buffers, waiting for the stream.  When the buffers of every segment the
+ * persistent kernel covers are page-locked and mapped into the device's
+ * address space (cudaHostAlloc / cudaHostRegister memory, 16-byte aligned),
+ * the zero-copy form of the persistent kernel reads and writes them directly
+ * over the host-device link, so inbound and outbound traffic overlap (one
+ * launch per storage type; h_in[i] == h_out[i] allowed); the other segments
+ * are copied through their device buffers.  Otherwise copies h_in[i] into
+ * segment i's device input, runs the batch (graph replay) and copies every
+ * segment's device output to h_out[i].  Not concurrent with other launches of
+ * the same batch. */
 int gbntt_batch_execute_host(gbntt_batch* batch, const void* const* h_in, void* const* h_out, void* stream);
 /* Rebinds a segment's buffers (no launch of the batch may be in flight). */
 int gbntt_batch_set_io(gbntt_batch* batch, uint32_t seg, const void* d_in, void* d_out);

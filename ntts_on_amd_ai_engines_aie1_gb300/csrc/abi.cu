@@ -150,6 +150,15 @@ void gbntt_internal_plan_args(const gbntt_plan* p, int* fam, int* L, int* elem_b
     *a = p->base;
 }
 
+const void* gbntt_internal_mapped(const void* h) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
+        cudaGetLastError();   // an unknown pointer is an answer, not an error
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 extern "C" {
 
 int gbntt_abi_version(void) { return GBNTT_ABI_VERSION; }

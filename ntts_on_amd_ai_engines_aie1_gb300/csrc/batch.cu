@@ -34,13 +34,14 @@ struct gbntt_batch {
         std::vector<Layout> layouts;    // candidate configurations
         int chosen = 0;
         std::vector<int> user_index;    // caller's segment of each SegDev
+        Layout zlay;                    // zero-copy launch (k_batch_zc), when a configuration has one
     };
     Part parts[2];
     int nparts = 0;
     std::vector<int> part_of;           // segment -> part (or -1: separate per-plan launch)
     std::vector<int> index_in_part;
     std::vector<gbntt_segment> user;    // the caller's segments
-    unsigned long long* d_ctr = nullptr;   // CTR_WORDS per part
+    unsigned long long* d_ctr = nullptr;   // CTR_WORDS per part; then CTR_WORDS per part for zero copy
     cudaGraphExec_t graph = nullptr;
 };
 
@@ -167,6 +168,11 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
                 part.layouts.push_back(lay);
             }
         if (flags & GBNTT_BATCH_NO_TUNE) part.layouts.resize(1);   // the first (widest, most specific) one
+        for (int c = 0; c < ncfg; ++c)                              // zero copy: first covering configuration
+            if (cfgs[c].zfn && (cfgs[c].set & part.fam_mask) == part.fam_mask) {
+                part.zlay.cfg = cfgs[c];
+                break;
+            }
     }
     for (int i = 0; i < b->nparts; ++i) {
       auto& part = b->parts[i];
@@ -174,7 +180,11 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
         const gbntt_segment& u = segs[pe.k];
         const int fam = pe.fam, L = pe.L, eb = pe.eb;
         const KArgs& a = pe.a;
-        for (auto& lay : part.layouts) {
+        std::vector<gbntt_batch::Layout*> lays;
+        for (auto& lay : part.layouts) lays.push_back(&lay);
+        if (part.zlay.cfg.zfn) lays.push_back(&part.zlay);
+        for (gbntt_batch::Layout* lp : lays) {
+            gbntt_batch::Layout& lay = *lp;
             const int elmax = lay.cfg.elmax;
             SegDev sd;
             std::memset(&sd, 0, sizeof(sd));
@@ -200,10 +210,15 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     for (int i = 0; i < b->nparts; ++i) {
-        for (auto& lay : b->parts[i].layouts) {
+        std::vector<gbntt_batch::Layout*> lays;
+        for (auto& lay : b->parts[i].layouts) lays.push_back(&lay);
+        if (b->parts[i].zlay.cfg.zfn) lays.push_back(&b->parts[i].zlay);
+        for (gbntt_batch::Layout* lp : lays) {
+            gbntt_batch::Layout& lay = *lp;
+            const bool zc = (lp == &b->parts[i].zlay);     // one staging buffer instead of two
             lay.stage_bytes = (lay.stage_bytes + 127) & ~127;
-            lay.smem = SMEM_HEADER + 2 * lay.stage_bytes + lay.smem;
-            const void* fn = lay.cfg.fn;
+            lay.smem = SMEM_HEADER + (zc ? 1 : 2) * lay.stage_bytes + lay.smem;
+            const void* fn = zc ? lay.cfg.zfn : lay.cfg.fn;
             cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, lay.smem);
             int per_sm = 0;
             if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BATCH_CTA, lay.smem);
@@ -221,8 +236,8 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
             }
         }
     }
-    cudaError_t e = cudaMalloc(&b->d_ctr, sizeof(unsigned long long) * CTR_WORDS * 2);
-    if (e == cudaSuccess) e = cudaMemset(b->d_ctr, 0, sizeof(unsigned long long) * CTR_WORDS * 2);
+    cudaError_t e = cudaMalloc(&b->d_ctr, sizeof(unsigned long long) * CTR_WORDS * 4);
+    if (e == cudaSuccess) e = cudaMemset(b->d_ctr, 0, sizeof(unsigned long long) * CTR_WORDS * 4);
     if (e != cudaSuccess) {
         gbntt_batch_destroy(b);
         return batch_fail(GBNTT_ERR_NOMEM, "batch scratch allocation failed");
@@ -285,6 +300,59 @@ int gbntt_batch_execute_host(gbntt_batch* b, const void* const* h_in, void* cons
         gbntt_plan_query(u.plan, GBNTT_Q_ELEM_BYTES, &eb);
         return (size_t)u.count * (size_t)n * (size_t)eb;
     };
+    // Zero copy: when every batched segment's host buffers are page-locked and
+    // mapped, one k_batch_zc launch per storage type reads and writes them in
+    // place, so inbound and outbound traffic overlap on the host-device link
+    // instead of running as two copy phases.  Segments outside the persistent
+    // kernel still go through their device buffers.
+    bool zero_copy = true;
+    for (size_t k = 0; k < b->user.size() && zero_copy; ++k) {
+        if (b->part_of[k] < 0 || !bytes_of(k)) continue;
+        const void* mi = gbntt_internal_mapped(h_in[k]);
+        const void* mo = gbntt_internal_mapped(h_out[k]);
+        zero_copy = b->parts[b->part_of[k]].zlay.cfg.zfn && mi && mo &&
+                    !((reinterpret_cast<uintptr_t>(mi) | reinterpret_cast<uintptr_t>(mo)) & 15);
+    }
+    if (zero_copy) {
+        for (int i = 0; i < b->nparts; ++i) {
+            auto& part = b->parts[i];
+            auto& lay = part.zlay;
+            if (!lay.total_tiles) continue;
+            std::vector<SegDev> segs = lay.segs;
+            for (size_t j = 0; j < segs.size(); ++j) {
+                const int k = part.user_index[j];
+                segs[j].a.in = gbntt_internal_mapped(h_in[k]);
+                segs[j].a.out = const_cast<void*>(gbntt_internal_mapped(h_out[k]));
+            }
+            cudaError_t e = cudaMemcpyAsync(lay.d_segs, segs.data(), sizeof(SegDev) * segs.size(),
+                                            cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("descriptors: ") + cudaGetErrorString(e));
+            BatchDev bd;
+            bd.segs = lay.d_segs;
+            bd.nsegs = (int)segs.size();
+            bd.total_tiles = lay.total_tiles;
+            bd.ctr = b->d_ctr + CTR_WORDS * (2 + i);
+            int sb = lay.stage_bytes;
+            void* args[] = {&bd, &sb};
+            e = cudaLaunchKernel(lay.cfg.zfn, dim3(lay.grid), dim3(BATCH_CTA), args, lay.smem, s);
+            if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("zero-copy launch: ") + cudaGetErrorString(e));
+            gbntt_internal_count_launch();
+        }
+        for (size_t k = 0; k < b->user.size(); ++k) {
+            const size_t bytes = bytes_of(k);
+            if (b->part_of[k] >= 0 || !bytes) continue;
+            const gbntt_segment& u = b->user[k];
+            cudaError_t e = cudaMemcpyAsync(const_cast<void*>(u.d_in), h_in[k], bytes, cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("H2D: ") + cudaGetErrorString(e));
+            const int rc = gbntt_execute(u.plan, u.d_in, u.d_out, u.count, s);
+            if (rc != GBNTT_OK) return rc;
+            e = cudaMemcpyAsync(h_out[k], u.d_out, bytes, cudaMemcpyDeviceToHost, s);
+            if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("D2H: ") + cudaGetErrorString(e));
+        }
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("synchronize: ") + cudaGetErrorString(e));
+        return GBNTT_OK;
+    }
     for (size_t k = 0; k < b->user.size(); ++k) {
         const size_t bytes = bytes_of(k);
         if (!bytes) continue;
@@ -364,9 +432,11 @@ int gbntt_batch_query(const gbntt_batch* b, int what, int64_t* value) {
 int gbntt_batch_destroy(gbntt_batch* b) {
     if (!b) return GBNTT_OK;
     if (b->graph) cudaGraphExecDestroy(b->graph);
-    for (int i = 0; i < b->nparts; ++i)
+    for (int i = 0; i < b->nparts; ++i) {
         for (auto& lay : b->parts[i].layouts)
             if (lay.d_segs) cudaFree(lay.d_segs);
+        if (b->parts[i].zlay.d_segs) cudaFree(b->parts[i].zlay.d_segs);
+    }
     if (b->d_ctr) cudaFree(b->d_ctr);
     delete b;
     return GBNTT_OK;

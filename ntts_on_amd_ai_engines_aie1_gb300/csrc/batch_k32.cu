@@ -6,7 +6,8 @@ namespace gbntt {
 namespace {
 constexpr int I32SET = (1 << F_R2F32) | (1 << F_R2G32);
 const BatchConfig kI32[] = {
-    {true, 5, I32SET, reinterpret_cast<const void*>(&k_batch<true, BATCH_CTA, 5, I32SET>)},
+    {true, 5, I32SET, reinterpret_cast<const void*>(&k_batch<true, BATCH_CTA, 5, I32SET>),
+     reinterpret_cast<const void*>(&k_batch_zc<true, BATCH_CTA, 5, I32SET>)},
 };
 }  // namespace
 

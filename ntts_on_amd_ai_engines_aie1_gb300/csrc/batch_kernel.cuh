@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(CTA, (I32 || ELMAX > 5) ? 2 : 3) k_batch(const
         switch (variant) {
 #define GB_CASE(F, L)                                                     \
     case variant_id(F, L):                                                \
-        if constexpr (fam_i32(F) == I32 && ((SET >> F) & 1)) tile_transform<F, L, CTA, ELMAX>(st, xbuf, kc, np); \
+        if constexpr (fam_i32(F) == I32 && ((SET >> F) & 1)) tile_transform<F, L, CTA, ELMAX>(st, xbuf, kc, *ka, np); \
         break;
             GB_I16_VARIANTS(GB_CASE)
             GB_I32_VARIANTS(GB_CASE)
@@ -147,6 +147,78 @@ __global__ void __launch_bounds__(CTA, (I32 || ELMAX > 5) ? 2 : 3) k_batch(const
     }
 }
 
+// Zero-copy form of the persistent kernel, for segments whose buffers are
+// page-locked host memory mapped into the device's address space: the same
+// tile loop and transform, but each tile moves with cooperative 16-byte loads
+// and stores (whole cache lines per warp, which the host-device link carries
+// efficiently) instead of bulk copies, with one staging buffer per CTA; the
+// CTAs resident on an SM overlap one another's transfers.
+template <bool I32, int CTA, int ELMAX, int SET>
+__global__ void __launch_bounds__(CTA, (I32 || ELMAX > 5) ? 2 : 3) k_batch_zc(const BatchDev b, int stage_bytes) {
+    extern __shared__ __align__(128) unsigned char bsmem[];
+    KArgs* ka = reinterpret_cast<KArgs*>(bsmem + 64);
+    unsigned char* stage = bsmem + SMEM_HEADER;
+    int* xbuf = reinterpret_cast<int*>(bsmem + SMEM_HEADER + stage_bytes);
+    __shared__ long long sh_next;
+    const int tid = threadIdx.x;
+    const long long total = b.total_tiles;
+    auto seg_of = [&](long long t) {
+        int s = 0;
+        while (s + 1 < b.nsegs && __ldg(&b.segs[s + 1].tile0) <= t) ++s;
+        return s;
+    };
+    if (tid == 0) sh_next = (long long)atomicAdd(&b.ctr[CTR_NEXT], 1ull);
+    __syncthreads();
+    long long t = sh_next;
+    int cur_seg = -1;
+    KC kc;
+    while (t < total) {
+        const int s = seg_of(t);
+        const SegDev* sd = &b.segs[s];
+        if (s != cur_seg) {
+            const int* src = reinterpret_cast<const int*>(&sd->a);
+            int* dst = reinterpret_cast<int*>(ka);
+            for (int w = tid; w < (int)(sizeof(KArgs) / 4); w += CTA) dst[w] = src[w];
+            cur_seg = s;
+            __syncthreads();
+            kc = make_kc(*ka);
+        }
+        const long long lt = t - sd->tile0;
+        const int P = sd->polys_per_tile;
+        const int np = (int)min((long long)P, sd->a.batch - lt * P);
+        const long long off = lt * P * (long long)sd->n * sd->elem_bytes;
+        const int words = np * sd->n * sd->elem_bytes / 16;
+        const uint4* gin = reinterpret_cast<const uint4*>(static_cast<const char*>(sd->a.in) + off);
+        uint4* st4 = reinterpret_cast<uint4*>(stage);
+        for (int i = tid; i < words; i += CTA) st4[i] = gin[i];
+        if (tid == 0) sh_next = (long long)atomicAdd(&b.ctr[CTR_NEXT], 1ull);
+        __syncthreads();
+        switch (sd->variant) {
+#define GB_CASE(F, L)                                                     \
+    case variant_id(F, L):                                                \
+        if constexpr (fam_i32(F) == I32 && ((SET >> F) & 1)) tile_transform<F, L, CTA, ELMAX>(stage, xbuf, kc, *ka, np); \
+        break;
+            GB_I16_VARIANTS(GB_CASE)
+            GB_I32_VARIANTS(GB_CASE)
+#undef GB_CASE
+            default: break;
+        }
+        __syncthreads();
+        uint4* gout = reinterpret_cast<uint4*>(static_cast<char*>(sd->a.out) + off);
+        for (int i = tid; i < words; i += CTA) gout[i] = st4[i];
+        t = sh_next;
+        __syncthreads();   // the stage is drained and sh_next read before the next tile
+    }
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(&b.ctr[CTR_DONE], 1ull) == (unsigned long long)gridDim.x - 1) {
+            b.ctr[CTR_NEXT] = 0;   // last CTA: rearm the tile counter for the next launch
+            b.ctr[CTR_DONE] = 0;
+            __threadfence();
+        }
+    }
+}
+
 inline bool variant_supported(int fam, int L) {
 #define GB_HAS(F, L_) if (fam == F && L == L_) return true;
     GB_I16_VARIANTS(GB_HAS)
@@ -162,10 +234,12 @@ struct BatchConfig {
     int elmax;   // log2 coefficients per thread
     int set;     // families covered (bit F)
     const void* fn;
+    const void* zfn;   // zero-copy form (k_batch_zc), or nullptr
 };
 
 // the configurations compiled into the library
 int batch_configs_i16(const BatchConfig** out);
+const void* batch_zc_kernel_i16(int set);   // k_batch_zc<int16, 32 coefficients per thread, set>
 int batch_configs_i32(const BatchConfig** out);
 
 }  // namespace gbntt

@@ -56,8 +56,7 @@ struct KC {
     const int* tab16;
     const int* f8;
     const int* ftail;
-    int q, c, fneg, wc, canonical, r8_sym, tail_wq, f1, f2, f3, wq1;
-    int natural_in, natural_out, scale, fb_fs, fb_wq;
+    int q, c, fneg, wc, r8_sym, tail_wq, f1, f2, f3, wq1;
 };
 
 __device__ __forceinline__ KC make_kc(const KArgs& a) {
@@ -71,12 +70,6 @@ __device__ __forceinline__ KC make_kc(const KArgs& a) {
     k.c = a.c;
     k.fneg = a.fneg;
     k.wc = a.wc;
-    k.canonical = a.canonical;
-    k.natural_in = a.natural_in;
-    k.natural_out = a.natural_out;
-    k.scale = a.scale;
-    k.fb_fs = a.fb_fs;
-    k.fb_wq = a.fb_wq;
     k.r8_sym = a.r8_sym;
     k.tail_wq = a.tail_wq;
     k.f1 = a.f8s[1];
@@ -149,12 +142,35 @@ __device__ __forceinline__ int canon(int x, int q) {
     return r < 0 ? r + q : r;
 }
 
-// the output epilogue shared by every kernel: fused n^-1 scaling, canonical form
-template <typename K>
-__device__ __forceinline__ int epilogue(int x, const K& a) {
-    if (a.scale) x = fb16(x, a.fb_fs, a.fb_wq, a.q);
-    if (a.canonical) x = canon(x, a.q);
-    return x;
+// Which output options a design accepts (checked by the host as well): the
+// fused n^-1 scaling belongs to the int16 inverse designs, natural-order input
+// to the inverse designs and natural-order output to the forward designs.
+// BR marks the radix-4 inverse, which runs the radix-4 kernel between two bit
+// reversals.  Gating them at compile time keeps their registers and code out
+// of the designs that never use them.
+__host__ __device__ constexpr bool fam_scales(int fam, bool br) { return fam == F_R2I16 || (fam == F_R4F16 && br); }
+__host__ __device__ constexpr bool fam_natural_in(int fam, bool br) {
+    return fam == F_R2I16 || fam == F_R2G32 || (fam == F_R4F16 && br);
+}
+__host__ __device__ constexpr bool fam_natural_out(int fam, bool br) { return !fam_natural_in(fam, br); }
+
+// The output epilogue: fused n^-1 scaling (SCALE designs), canonical form.
+// The flags are read from the kernel arguments where they are used, so they
+// hold no registers through the transform.
+template <bool SCALE, int E>
+__device__ __forceinline__ void epilogue_all(int (&v)[E], const KArgs& a) {
+    if constexpr (SCALE) {
+        if (a.scale) {
+            const int fs = a.fb_fs, wq = a.fb_wq, q = a.q;
+#pragma unroll
+            for (int k = 0; k < E; ++k) v[k] = fb16(v[k], fs, wq, q);
+        }
+    }
+    if (a.canonical) {
+        const int q = a.q;
+#pragma unroll
+        for (int k = 0; k < E; ++k) v[k] = canon(v[k], q);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -468,38 +484,38 @@ __device__ __forceinline__ void run_steps_x(int (&v)[1 << EL], int* sp, int g, c
 // load / store of one polynomial in a window layout
 // ---------------------------------------------------------------------------
 
-template <bool I32, int L, int EL, int LO>
-__device__ __forceinline__ void load_poly_br(int (&v)[1 << EL], const KArgs& a, long long poly, int g) {
-    constexpr int E = 1 << EL;
-    constexpr long long N = 1LL << L;
+// Bit-reversal permutation of one polynomial held in the window layout LO:
+// afterwards the register of position p holds the value that was at position
+// bitrev_L(p).  Within one thread (L == EL) it is a renaming of registers;
+// otherwise it goes through the polynomial's exchange buffer, so the global
+// accesses around it stay coalesced.
+template <int L, int EL, int LO>
+__device__ __forceinline__ void permute_br(int (&v)[1 << EL], int* sp, int g) {
+    constexpr int E = 1 << EL, G = 1 << (L - EL);
+    if constexpr (G == 1) {
+        int t[E];
 #pragma unroll
-    for (int k = 0; k < E; ++k) {
-        const int p = (int)(__brev((unsigned)posmap<LO, EL>(g, k)) >> (32 - L));
-        if constexpr (I32) v[k] = __ldg(static_cast<const int*>(a.in) + poly * N + p);
-        else v[k] = (int)__ldg(static_cast<const short*>(a.in) + poly * N + p);
+        for (int k = 0; k < E; ++k) t[k] = v[k];
+#pragma unroll
+        for (int k = 0; k < E; ++k) v[k] = t[brev_c<L>(k)];
+    } else {
+        // the thread bits and the register bits of a position are disjoint, so
+        // bitrev(pos) = bitrev(thread part) | bitrev(register part), and spad
+        // splits the same way: one runtime base plus a constant per register
+        const int base = spad((int)(__brev((unsigned)posmap<LO, EL>(g, 0)) >> (32 - L)));
+        group_sync<G>();
+#pragma unroll
+        for (int k = 0; k < E; ++k) sp[base + spad(brev_c<L>(k << LO))] = v[k];
+        group_sync<G>();
+#pragma unroll
+        for (int k = 0; k < E; ++k) v[k] = sp[spad(posmap<LO, EL>(g, k))];
     }
 }
 
 template <bool I32, int L, int EL, int LO>
-__device__ __forceinline__ void store_poly_br(int (&v)[1 << EL], const KArgs& a, long long poly, int g) {
-    constexpr int E = 1 << EL;
-    constexpr long long N = 1LL << L;
-#pragma unroll
-    for (int k = 0; k < E; ++k) {
-        const int p = (int)(__brev((unsigned)posmap<LO, EL>(g, k)) >> (32 - L));
-        if constexpr (I32) static_cast<int*>(a.out)[poly * N + p] = v[k];
-        else static_cast<short*>(a.out)[poly * N + p] = (short)v[k];
-    }
-}
-
-template <bool I32, int L, int EL, int LO, bool BR>
 __device__ __forceinline__ void load_poly(int (&v)[1 << EL], const KArgs& a, long long poly, int g) {
     constexpr int E = 1 << EL;
     constexpr long long N = 1LL << L;
-    if (BR != (a.natural_in != 0)) {
-        load_poly_br<I32, L, EL, LO>(v, a, poly, g);
-        return;
-    }
     if constexpr (I32) {
         const int* src = static_cast<const int*>(a.in) + poly * N;
         if constexpr (LO == 0 && E >= 4) {
@@ -538,18 +554,10 @@ __device__ __forceinline__ void load_poly(int (&v)[1 << EL], const KArgs& a, lon
     }
 }
 
-template <bool I32, int L, int EL, int LO, bool BR>
+template <bool I32, int L, int EL, int LO>
 __device__ __forceinline__ void store_poly(int (&v)[1 << EL], const KArgs& a, long long poly, int g) {
     constexpr int E = 1 << EL;
     constexpr long long N = 1LL << L;
-    if (a.scale || a.canonical) {
-#pragma unroll
-        for (int k = 0; k < E; ++k) v[k] = epilogue(v[k], a);
-    }
-    if (BR != (a.natural_out != 0)) {
-        store_poly_br<I32, L, EL, LO>(v, a, poly, g);
-        return;
-    }
     if constexpr (I32) {
         int* dst = static_cast<int*>(a.out) + poly * N;
         if constexpr (LO == 0 && E >= 4) {
@@ -604,14 +612,27 @@ __global__ void __launch_bounds__(P << (L - EL)) k_ntt(const __grid_constant__ K
     constexpr int LO0 = window_lo(FAM, L, EL, 0);
     constexpr int LOZ = window_lo(FAM, L, EL, NS - 1);
     if (active) {
-        load_poly<I32, L, EL, LO0, BR>(v, a, poly, g);
+        load_poly<I32, L, EL, LO0>(v, a, poly, g);
     } else {
 #pragma unroll
         for (int k = 0; k < (1 << EL); ++k) v[k] = 0;
     }
+    // bit-reversed input: the radix-4 inverse reads bit-reversed order unless
+    // the input is natural; the other inverse designs read natural order on request
+    if constexpr (BR) {
+        if (!a.natural_in) permute_br<L, EL, LO0>(v, sp, g);
+    } else if constexpr (fam_natural_in(FAM, BR)) {
+        if (a.natural_in) permute_br<L, EL, LO0>(v, sp, g);
+    }
     const KC kc = make_kc(a);
     run_steps<FAM, L, EL>(v, sp, g, kc, std::make_integer_sequence<int, NS>{});
-    if (active) store_poly<I32, L, EL, LOZ, BR>(v, a, poly, g);
+    epilogue_all<fam_scales(FAM, BR)>(v, a);
+    if constexpr (BR) {
+        permute_br<L, EL, LOZ>(v, sp, g);
+    } else if constexpr (fam_natural_out(FAM, BR)) {
+        if (a.natural_out) permute_br<L, EL, LOZ>(v, sp, g);
+    }
+    if (active) store_poly<I32, L, EL, LOZ>(v, a, poly, g);
 }
 
 struct KernelInfo {

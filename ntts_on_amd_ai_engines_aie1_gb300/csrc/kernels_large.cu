@@ -36,9 +36,10 @@ __global__ void __launch_bounds__(COLS << (L1 - LARGE_EL)) k_cols(const __grid_c
     for (int k = 0; k < E; ++k) v[k] = __ldg(in + ((long long)posmap<LO0, EL>(g, k) << L2));
     const KC kc = make_kc(a);
     run_steps_x<FAM, L1, EL, COLS, false>(v, csmem, g, kc, 0, cl, std::make_integer_sequence<int, NS>{});
+    epilogue_all<false>(v, a);
     __syncthreads();   // every read of `in` is done before an in-place store lands
 #pragma unroll
-    for (int k = 0; k < E; ++k) out[(long long)posmap<LOZ, EL>(g, k) << L2] = epilogue(v[k], kc);
+    for (int k = 0; k < E; ++k) out[(long long)posmap<LOZ, EL>(g, k) << L2] = v[k];
 }
 
 // one CTA: P rows of 2^L2 coefficients, G threads per row
@@ -63,10 +64,11 @@ __global__ void __launch_bounds__(P << (L2 - LARGE_EL)) k_rows(const __grid_cons
     }
     const KC kc = make_kc(a);
     run_steps_x<FAM, L2, EL, 0, true>(v, sp, g, kc, hi, 0, std::make_integer_sequence<int, NS>{});
+    epilogue_all<false>(v, a);
     if (active) {
         int* dst = static_cast<int*>(a.out) + row * N;
 #pragma unroll
-        for (int k = 0; k < E; ++k) dst[posmap<LOZ, EL>(g, k)] = epilogue(v[k], kc);
+        for (int k = 0; k < E; ++k) dst[posmap<LOZ, EL>(g, k)] = v[k];
     }
 }
 

@@ -53,7 +53,8 @@ __global__ void __launch_bounds__(256) k_r8_stage(const KArgs a, int L) {
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             const int2 t = __ldg(&a.tab[k * M + i]);
-            const int z = epilogue(r8red(y[k], t.x, t.y, a.q), a);
+            int z = r8red(y[k], t.x, t.y, a.q);
+            if (a.canonical) z = canon(z, a.q);
             o[brev_c<3>(k)] = z;
         }
         int4 w;

@@ -107,8 +107,25 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 // one tile: P polynomials staged contiguously in shared memory
 // ---------------------------------------------------------------------------
 
+// reads one staged polynomial into the window layout LOS; BRV: the staged
+// polynomial is in natural order and the transform wants it bit-reversed
+template <bool I32, int L, int EL, int LOS, bool BRV>
+__device__ __forceinline__ void stage_read(int (&v)[1 << EL], const void* stage, int lp, int g) {
+    constexpr int E = 1 << EL, N = 1 << L;
+    // bitrev of a position = bitrev(thread bits) | bitrev(register bits)
+    const int base = lp * N + (BRV ? (int)(__brev((unsigned)posmap<LOS, EL>(g, 0)) >> (32 - L)) : 0);
+#pragma unroll
+    for (int k = 0; k < E; ++k) {
+        const int p = BRV ? base + brev_c<L>(k << LOS) : lp * N + posmap<LOS, EL>(g, k);
+        if constexpr (I32) v[k] = static_cast<const int*>(stage)[p];
+        else v[k] = static_cast<const short*>(stage)[p];
+    }
+}
+
+// ka: the segment's arguments in shared memory, read only where the output
+// options are applied (natural order, n^-1 scaling, canonical form)
 template <int FAM, int L, int CTA, int ELMAX>
-__device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KC& a, int npolys) {
+__device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KC& a, const KArgs& ka, int npolys) {
     constexpr int EL = batch_el(L, ELMAX);
     constexpr int G = 1 << (L - EL), N = 1 << L, E = 1 << EL;
     constexpr int SW = xwords(L);
@@ -125,21 +142,11 @@ __device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KC&
     int v[E];
     if (active) {
         // natural-order input of an inverse design: the bit reversal is the read pattern
-        const unsigned br = a.natural_in ? 0xFFFFFFFFu : 0u;
-        if constexpr (I32) {
-            const int* s = static_cast<const int*>(stage) + lp * N;
-#pragma unroll
-            for (int k = 0; k < E; ++k) {
-                const int p = posmap<LOS, EL>(g, k);
-                v[k] = s[br ? (int)(__brev((unsigned)p) >> (32 - L)) : p];
-            }
+        if constexpr (fam_natural_in(FAM, false)) {
+            if (ka.natural_in) stage_read<I32, L, EL, LOS, true>(v, stage, lp, g);
+            else stage_read<I32, L, EL, LOS, false>(v, stage, lp, g);
         } else {
-            const short* s = static_cast<const short*>(stage) + lp * N;
-#pragma unroll
-            for (int k = 0; k < E; ++k) {
-                const int p = posmap<LOS, EL>(g, k);
-                v[k] = s[br ? (int)(__brev((unsigned)p) >> (32 - L)) : p];
-            }
+            stage_read<I32, L, EL, LOS, false>(v, stage, lp, g);
         }
     } else {
 #pragma unroll
@@ -147,20 +154,20 @@ __device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KC&
     }
     if constexpr (LO0 != LOS) exchange_windows<L, EL, LOS, LO0>(v, sp, g);
     run_steps<FAM, L, EL>(v, sp, g, a, std::make_integer_sequence<int, NS>{});
-    if (a.scale || a.canonical) {
-#pragma unroll
-        for (int k = 0; k < E; ++k) v[k] = epilogue(v[k], a);
-    }
+    epilogue_all<fam_scales(FAM, false)>(v, ka);
     if (!active) return;
-    if (a.natural_out) {
-        // natural-order output of a forward design: bit-reversed scatter into the tile
+    if constexpr (fam_natural_out(FAM, false)) {
+        if (ka.natural_out) {
+            // natural-order output of a forward design: bit-reversed scatter into the tile
+            const int base = lp * N + (int)(__brev((unsigned)posmap<LOZ, EL>(g, 0)) >> (32 - L));
 #pragma unroll
-        for (int k = 0; k < E; ++k) {
-            const int p = (int)(__brev((unsigned)posmap<LOZ, EL>(g, k)) >> (32 - L));
-            if constexpr (I32) static_cast<int*>(stage)[lp * N + p] = v[k];
-            else static_cast<short*>(stage)[lp * N + p] = (short)v[k];
+            for (int k = 0; k < E; ++k) {
+                const int p = base + brev_c<L>(k << LOZ);
+                if constexpr (I32) static_cast<int*>(stage)[p] = v[k];
+                else static_cast<short*>(stage)[p] = (short)v[k];
+            }
+            return;
         }
-        return;
     }
     if constexpr (LOZ == 0 && (I32 ? E >= 4 : E >= 8)) {
         // thread owns E consecutive coefficients: 16-byte stores

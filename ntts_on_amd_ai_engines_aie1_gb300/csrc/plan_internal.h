@@ -12,3 +12,9 @@ void gbntt_internal_count_launch();
 int gbntt_internal_plan_L(const gbntt_plan* p);
 // family (-1 when the design has no persistent-kernel variant), log2 n, element bytes, launch constants
 void gbntt_internal_plan_args(const gbntt_plan* p, int* fam, int* L, int* elem_bytes, gbntt::KArgs* a);
+// Device address of a page-locked host buffer that is mapped into the device's
+// address space (cudaHostAlloc / cudaHostRegister memory under unified
+// addressing), or nullptr for any other pointer.  A buffer with such an address
+// can be read and written by the transform kernels directly over the
+// host-device link (zero copy).
+const void* gbntt_internal_mapped(const void* h);

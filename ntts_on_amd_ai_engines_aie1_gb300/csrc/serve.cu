@@ -7,8 +7,17 @@
 //     the whole arena are refused;
 //   * micro-batches: the admitted requests that are waiting when a stream
 //     slot is free are grouped by plan; each plan group gets one contiguous
-//     arena block, its inputs are copied in, one in-place launch transforms
-//     the group, the outputs are copied back, and an event closes the slot;
+//     arena block and its inputs are copied in; one in-place launch of the
+//     persistent kernel per storage type transforms every group at once (one
+//     segment per group; int32 transforms of n >= 2^16 run their plan's
+//     two-pass launches); the outputs are copied back and an event closes
+//     the slot;
+//   * copies: requests whose host buffers are page-locked and mapped into the
+//     device's address space move through one gather kernel (host -> arena)
+//     and one scatter kernel (arena -> host) per micro-batch, driven by a
+//     descriptor table uploaded with one copy, so the host issues a handful of
+//     calls per micro-batch instead of two per request; other requests use
+//     one cudaMemcpyAsync per direction;
 //   * while slots are busy on the GPU, newly arrived requests are admitted
 //     into the next micro-batch, so copies and kernels of different
 //     micro-batches overlap on the device;
@@ -31,6 +40,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/gb300_ntt.h"
+#include "batch_kernel.cuh"
 #include "plan_internal.h"
 
 namespace gbntt {
@@ -116,7 +126,45 @@ struct Request {
     uint64_t count;
     size_t bytes;
     Clock::time_point t_submit;
+    const void* m_in;   // device addresses of mapped host buffers (nullptr: copy engine)
+    void* m_out;
 };
+
+// one host<->arena copy of the gather/scatter kernels, cut into COPY_CHUNK pieces
+struct CopyDesc {
+    const unsigned char* src;
+    unsigned char* dst;
+    unsigned long long bytes;
+    unsigned long long chunk0;   // first chunk index of this copy
+};
+constexpr unsigned long long COPY_CHUNK = 16384;
+constexpr int COPY_THREADS = 256;
+
+// block c copies chunk c: it finds its descriptor by binary search over chunk0
+__global__ void __launch_bounds__(COPY_THREADS) k_copy_desc(const CopyDesc* __restrict__ d, int nd) {
+    const unsigned long long c = blockIdx.x;
+    int lo = 0, hi = nd - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (d[mid].chunk0 <= c) lo = mid;
+        else hi = mid - 1;
+    }
+    const unsigned long long off = (c - d[lo].chunk0) * COPY_CHUNK;
+    const unsigned long long rem = d[lo].bytes - off;
+    const unsigned len = (unsigned)(rem < COPY_CHUNK ? rem : COPY_CHUNK);
+    const unsigned char* s = d[lo].src + off;
+    unsigned char* t = d[lo].dst + off;
+    const unsigned long long mis = reinterpret_cast<unsigned long long>(s) | reinterpret_cast<unsigned long long>(t) | len;
+    if (!(mis & 15)) {
+        for (unsigned i = threadIdx.x; i < len / 16; i += COPY_THREADS)
+            reinterpret_cast<uint4*>(t)[i] = reinterpret_cast<const uint4*>(s)[i];
+    } else if (!(mis & 3)) {
+        for (unsigned i = threadIdx.x; i < len / 4; i += COPY_THREADS)
+            reinterpret_cast<unsigned*>(t)[i] = reinterpret_cast<const unsigned*>(s)[i];
+    } else {
+        for (unsigned i = threadIdx.x; i < len; i += COPY_THREADS) t[i] = s[i];
+    }
+}
 
 struct Group {                  // one plan's requests in one micro-batch
     uint32_t plan;
@@ -130,6 +178,25 @@ struct Slot {
     cudaEvent_t done = nullptr;
     bool busy = false;
     std::vector<Group> groups;
+    CopyDesc* h_desc = nullptr;   // page-locked descriptor table: gather copies, then scatter copies
+    CopyDesc* d_desc = nullptr;
+    SegDev* h_seg = nullptr;      // page-locked segment descriptors: int16 part, then int32 part
+    SegDev* d_seg = nullptr;
+    unsigned long long* d_ctr = nullptr;   // tile counters of the two persistent launches
+    unsigned long long* h_err = nullptr;   // their error words, read back with the results
+};
+
+// a plan as the persistent kernel sees it
+struct PlanInfo {
+    int fam = -1, L = 0, eb = 0;
+    gbntt::KArgs a;
+    int part = -1;   // 0 int16 / 1 int32 persistent launch, -1: the plan's own launches
+};
+
+// one persistent launch configuration per storage type
+struct PartCfg {
+    const gbntt::BatchConfig* cfg = nullptr;
+    int stage = 0, smem = 0, grid = 0;
 };
 
 }  // namespace
@@ -137,6 +204,8 @@ struct Slot {
 struct gbntt_server {
     std::vector<const gbntt_plan*> plans;
     std::vector<int64_t> plan_bytes;   // bytes of one polynomial
+    std::vector<PlanInfo> pinfo;
+    PartCfg part[2];
     std::vector<Slot> slots;
     Arena arena;
     char* d_arena = nullptr;
@@ -167,6 +236,12 @@ int sfail(int code, const std::string& m) { return gbntt_internal_fail(code, m);
 void finish_slot(gbntt_server* s, Slot& sl) {
     const auto now = Clock::now();
     std::lock_guard<std::mutex> lk(s->mu);
+    if (sl.h_err[CTR_ERROR] || sl.h_err[CTR_WORDS + CTR_ERROR]) {
+        // a tile load did not arrive within the persistent kernel's wait limit
+        s->worker_error = GBNTT_ERR_TIMEOUT;
+        s->worker_msg = "serve: a tile load did not arrive within the wait limit";
+        s->stop = true;
+    }
     for (auto& g : sl.groups) {
         s->arena.release(g.off, g.bytes);
         for (auto& r : g.reqs) {
@@ -183,27 +258,135 @@ void finish_slot(gbntt_server* s, Slot& sl) {
     s->cv_work.notify_all();
 }
 
-// Issue one micro-batch on slot sl (copies in, one launch per plan group, copies out).
+// Issue one micro-batch on slot sl: gather (kernel for mapped requests, copy
+// engine for the others), one in-place launch per plan group, scatter, event.
 int issue(gbntt_server* s, Slot& sl) {
+    int nin = 0;
+    unsigned long long cin = 0;
+    for (auto& g : sl.groups) {               // gather descriptors
+        size_t at = 0;
+        for (auto& r : g.reqs) {
+            if (r.m_in) {
+                sl.h_desc[nin++] = CopyDesc{static_cast<const unsigned char*>(r.m_in),
+                                            reinterpret_cast<unsigned char*>(s->d_arena + g.off + at), r.bytes, cin};
+                cin += (r.bytes + COPY_CHUNK - 1) / COPY_CHUNK;
+            }
+            at += r.bytes;
+        }
+    }
+    int nout = 0;
+    unsigned long long cout = 0;
+    CopyDesc* od = sl.h_desc + nin;
+    for (auto& g : sl.groups) {               // scatter descriptors
+        size_t at = 0;
+        for (auto& r : g.reqs) {
+            if (r.m_out) {
+                od[nout++] = CopyDesc{reinterpret_cast<const unsigned char*>(s->d_arena + g.off + at),
+                                      static_cast<unsigned char*>(r.m_out), r.bytes, cout};
+                cout += (r.bytes + COPY_CHUNK - 1) / COPY_CHUNK;
+            }
+            at += r.bytes;
+        }
+    }
+    cudaError_t e;
+    if (nin + nout) {
+        e = cudaMemcpyAsync(sl.d_desc, sl.h_desc, (size_t)(nin + nout) * sizeof(CopyDesc), cudaMemcpyHostToDevice,
+                            sl.stream);
+        if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve descriptors: ") + cudaGetErrorString(e));
+    }
+    if (nin) {
+        k_copy_desc<<<(unsigned)cin, COPY_THREADS, 0, sl.stream>>>(sl.d_desc, nin);
+        gbntt_internal_count_launch();
+        ++s->launches;
+    }
     for (auto& g : sl.groups) {
         char* base = s->d_arena + g.off;
         size_t at = 0;
         for (auto& r : g.reqs) {
-            cudaError_t e = cudaMemcpyAsync(base + at, r.h_in, r.bytes, cudaMemcpyHostToDevice, sl.stream);
-            if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve H2D: ") + cudaGetErrorString(e));
-            at += r.bytes;
-        }
-        const int rc = gbntt_execute(s->plans[g.plan], base, base, g.count, sl.stream);
-        if (rc != GBNTT_OK) return rc;
-        ++s->launches;
-        at = 0;
-        for (auto& r : g.reqs) {
-            cudaError_t e = cudaMemcpyAsync(r.h_out, base + at, r.bytes, cudaMemcpyDeviceToHost, sl.stream);
-            if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve D2H: ") + cudaGetErrorString(e));
+            if (!r.m_in) {
+                e = cudaMemcpyAsync(base + at, r.h_in, r.bytes, cudaMemcpyHostToDevice, sl.stream);
+                if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve H2D: ") + cudaGetErrorString(e));
+            }
             at += r.bytes;
         }
     }
-    cudaError_t e = cudaEventRecord(sl.done, sl.stream);
+    // one persistent launch per storage type over all groups, largest n first
+    {
+        std::vector<const Group*> order;
+        for (auto& g : sl.groups) order.push_back(&g);
+        std::stable_sort(order.begin(), order.end(), [&](const Group* x, const Group* y) {
+            return s->pinfo[x->plan].L > s->pinfo[y->plan].L;
+        });
+        const int cap = (int)s->plans.size();
+        int nseg[2] = {0, 0};
+        long long tiles[2] = {0, 0};
+        for (const Group* g : order) {
+            const PlanInfo& pi = s->pinfo[g->plan];
+            if (pi.part < 0) continue;
+            SegDev& sd = sl.h_seg[pi.part * cap + nseg[pi.part]++];
+            std::memset(&sd, 0, sizeof(sd));
+            sd.a = pi.a;
+            sd.a.in = s->d_arena + g->off;
+            sd.a.out = s->d_arena + g->off;
+            sd.a.batch = (long long)g->count;
+            sd.n = 1 << pi.L;
+            sd.elem_bytes = pi.eb;
+            sd.variant = variant_id(pi.fam, pi.L);
+            sd.polys_per_tile = BATCH_CTA >> (pi.L - batch_el(pi.L, s->part[pi.part].cfg->elmax));
+            sd.tiles = (sd.a.batch + sd.polys_per_tile - 1) / sd.polys_per_tile;
+            sd.tile0 = tiles[pi.part];
+            tiles[pi.part] += sd.tiles;
+        }
+        for (int p = 0; p < 2; ++p) {
+            if (!nseg[p]) continue;
+            e = cudaMemcpyAsync(sl.d_seg + p * cap, sl.h_seg + p * cap, sizeof(SegDev) * nseg[p],
+                                cudaMemcpyHostToDevice, sl.stream);
+            if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve segments: ") + cudaGetErrorString(e));
+            const PartCfg& pc = s->part[p];
+            BatchDev bd;
+            bd.segs = sl.d_seg + p * cap;
+            bd.nsegs = nseg[p];
+            bd.total_tiles = tiles[p];
+            bd.ctr = sl.d_ctr + CTR_WORDS * p;
+            int sb = pc.stage;
+            void* args[] = {&bd, &sb};
+            const unsigned grid = (unsigned)std::min<long long>(pc.grid, tiles[p]);
+            e = cudaLaunchKernel(pc.cfg->fn, dim3(grid), dim3(BATCH_CTA), args, pc.smem, sl.stream);
+            if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve launch: ") + cudaGetErrorString(e));
+            gbntt_internal_count_launch();
+            ++s->launches;
+        }
+        for (const Group* g : order) {
+            if (s->pinfo[g->plan].part >= 0) continue;
+            const int rc = gbntt_execute(s->plans[g->plan], s->d_arena + g->off, s->d_arena + g->off, g->count,
+                                         sl.stream);
+            if (rc != GBNTT_OK) return rc;
+            ++s->launches;
+        }
+        // the persistent launches' error words come back with the results
+        e = cudaMemcpyAsync(sl.h_err, sl.d_ctr, 2 * CTR_WORDS * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                            sl.stream);
+        if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve status: ") + cudaGetErrorString(e));
+    }
+    if (nout) {
+        k_copy_desc<<<(unsigned)cout, COPY_THREADS, 0, sl.stream>>>(sl.d_desc + nin, nout);
+        gbntt_internal_count_launch();
+        ++s->launches;
+    }
+    for (auto& g : sl.groups) {
+        char* base = s->d_arena + g.off;
+        size_t at = 0;
+        for (auto& r : g.reqs) {
+            if (!r.m_out) {
+                e = cudaMemcpyAsync(r.h_out, base + at, r.bytes, cudaMemcpyDeviceToHost, sl.stream);
+                if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve D2H: ") + cudaGetErrorString(e));
+            }
+            at += r.bytes;
+        }
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve copy kernel: ") + cudaGetErrorString(e));
+    e = cudaEventRecord(sl.done, sl.stream);
     if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve event: ") + cudaGetErrorString(e));
     sl.busy = true;
     ++s->microbatches;
@@ -316,6 +499,49 @@ int gbntt_server_create(gbntt_server** out, const gbntt_plan* const* plans, uint
             return sfail(GBNTT_ERR_ARG, "the radix-8 stage cannot run in place and is not served");
         }
         s->plan_bytes.push_back(n * eb);
+        PlanInfo pi;
+        gbntt_internal_plan_args(p, &pi.fam, &pi.L, &pi.eb, &pi.a);
+        if (pi.fam >= 0 && variant_supported(pi.fam, pi.L)) pi.part = fam_i32(pi.fam) ? 1 : 0;
+        s->pinfo.push_back(pi);
+    }
+    // per storage type: the first 32-coefficient configuration covering the served families
+    {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        for (int p = 0; p < 2; ++p) {
+            int mask = 0, stage = 0, xbytes = 0;
+            for (const auto& pi : s->pinfo)
+                if (pi.part == p) mask |= 1 << pi.fam;
+            if (!mask) continue;
+            const BatchConfig* cfgs = nullptr;
+            const int ncfg = p ? batch_configs_i32(&cfgs) : batch_configs_i16(&cfgs);
+            const BatchConfig* cfg = nullptr;
+            for (int c = 0; c < ncfg && !cfg; ++c)
+                if (cfgs[c].elmax == 5 && (cfgs[c].set & mask) == mask) cfg = &cfgs[c];
+            if (!cfg) {   // no persistent kernel covers them: the plans launch on their own
+                for (auto& pi : s->pinfo)
+                    if (pi.part == p) pi.part = -1;
+                continue;
+            }
+            for (const auto& pi : s->pinfo) {
+                if (pi.part != p) continue;
+                stage = std::max(stage, batch_stage_bytes(BATCH_CTA, pi.L, pi.eb, cfg->elmax));
+                xbytes = std::max(xbytes, batch_xbuf_bytes(BATCH_CTA, pi.L, cfg->elmax));
+            }
+            PartCfg& pc = s->part[p];
+            pc.cfg = cfg;
+            pc.stage = (stage + 127) & ~127;
+            pc.smem = SMEM_HEADER + 2 * pc.stage + xbytes;
+            int per_sm = 0;
+            cudaError_t e = cudaFuncSetAttribute(cfg->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pc.smem);
+            if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cfg->fn, BATCH_CTA, pc.smem);
+            if (e != cudaSuccess || per_sm < 1) {
+                delete s;
+                return sfail(GBNTT_ERR_CUDA, std::string("serve kernel configuration: ") + cudaGetErrorString(e));
+            }
+            pc.grid = per_sm * sms;
+        }
     }
     const uint32_t nslots = cfg && cfg->slots ? cfg->slots : 4;
     s->max_group_requests = cfg && cfg->max_requests_per_batch ? cfg->max_requests_per_batch : 4096;
@@ -343,6 +569,19 @@ int gbntt_server_create(gbntt_server** out, const gbntt_plan* const* plans, uint
     for (auto& sl : s->slots) {
         cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
         cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+        const size_t db = 2 * (size_t)s->max_group_requests * sizeof(CopyDesc);
+        const size_t sb = 2 * s->plans.size() * sizeof(SegDev);
+        const size_t cb = 2 * CTR_WORDS * sizeof(unsigned long long);
+        if (cudaHostAlloc(&sl.h_desc, db, cudaHostAllocDefault) != cudaSuccess ||
+            cudaMalloc(&sl.d_desc, db) != cudaSuccess ||
+            cudaHostAlloc(&sl.h_seg, sb, cudaHostAllocDefault) != cudaSuccess ||
+            cudaMalloc(&sl.d_seg, sb) != cudaSuccess ||
+            cudaHostAlloc(&sl.h_err, cb, cudaHostAllocDefault) != cudaSuccess ||
+            cudaMalloc(&sl.d_ctr, cb) != cudaSuccess || cudaMemset(sl.d_ctr, 0, cb) != cudaSuccess) {
+            cudaGetLastError();
+            gbntt_server_destroy(s);
+            return sfail(GBNTT_ERR_NOMEM, "descriptor tables allocation failed");
+        }
     }
     s->t_first = s->t_last = Clock::now();
     s->worker = std::thread(worker_main, s);
@@ -356,6 +595,8 @@ int gbntt_server_submit(gbntt_server* s, uint32_t plan, const void* h_in, void* 
     if (plan >= s->plans.size()) return sfail(GBNTT_ERR_ARG, "plan index out of range");
     if (!h_in || !h_out || !count) return sfail(GBNTT_ERR_ARG, "request without data");
     const size_t bytes = (size_t)count * (size_t)s->plan_bytes[plan];
+    const void* m_in = gbntt_internal_mapped(h_in);
+    void* m_out = const_cast<void*>(gbntt_internal_mapped(h_out));
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->worker_error) return sfail(s->worker_error, s->worker_msg);
     const uint64_t t = s->next_ticket++;
@@ -367,7 +608,7 @@ int gbntt_server_submit(gbntt_server* s, uint32_t plan, const void* h_in, void* 
         return GBNTT_OK;
     }
     if (s->completed == 0 && s->pending.empty() && s->microbatches == 0) s->t_first = Clock::now();
-    s->pending.push_back(Request{t, plan, h_in, h_out, count, bytes, Clock::now()});
+    s->pending.push_back(Request{t, plan, h_in, h_out, count, bytes, Clock::now(), m_in, m_out});
     s->cv_work.notify_one();
     return GBNTT_OK;
 }
@@ -442,6 +683,12 @@ int gbntt_server_destroy(gbntt_server* s) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
         if (sl.done) cudaEventDestroy(sl.done);
         if (sl.stream) cudaStreamDestroy(sl.stream);
+        if (sl.h_desc) cudaFreeHost(sl.h_desc);
+        if (sl.d_desc) cudaFree(sl.d_desc);
+        if (sl.h_seg) cudaFreeHost(sl.h_seg);
+        if (sl.d_seg) cudaFree(sl.d_seg);
+        if (sl.h_err) cudaFreeHost(sl.h_err);
+        if (sl.d_ctr) cudaFree(sl.d_ctr);
     }
     if (s->d_arena) cudaFree(s->d_arena);
     delete s;

@@ -238,6 +238,65 @@ def test_execute_host(gb, orc):
     assert np.array_equal(out, orc.Plan(orc.R8_I16_STAGE, n, q, root_for(q, n))(x))
 
 
+HOST_CASES = [  # (kind, n, q, factor, flags, dtype) -- every design
+    (0, 1024, 12289, 0, 0, np.int16), (1, 1024, 12289, 0, 0x8 | 0x10, np.int16), (2, 256, 7681, 0, 0, np.int16),
+    (9, 4096, 12289, 0, 0, np.int16), (3, 512, 12289, 0, 0, np.int16), (8, 2048, 12289, 0, 0x8, np.int16),
+    (6, 1024, 0, 0, 0, np.int16), (7, 1024, 12289, 12277, 0, np.int16), (4, 4096, 998244353, 0, 0x1, np.int32),
+    (5, 2048, 754974721, 0, 0x8, np.int32), (4, 1 << 16, 469762049, 0, 0, np.int32)]
+
+
+@pytest.mark.parametrize("kind,n,q,factor,flags,dt", HOST_CASES)
+def test_execute_host_every_design(gb, kind, n, q, factor, flags, dt):
+    """Host buffers, pinned and pageable, equal the device-memory launch, also in place."""
+    root = root_for(q, n) if q and kind != 7 else 0
+    plan = gb.Plan(kind, n, q, root, factor, flags)
+    rng = np.random.default_rng(SEED + 77 + kind + n)
+    lo, hi = (0, q) if q else (-32768, 32768)
+    x = rng.integers(lo, hi, (5, n)).astype(dt)
+    want = plan(torch.from_numpy(x).cuda()).cpu().numpy()
+    pin_in = torch.from_numpy(x).pin_memory()
+    pin_out = torch.empty_like(pin_in).pin_memory()
+    plan.execute_host(pin_in, pin_out)
+    assert np.array_equal(pin_out.numpy(), want)
+    page_out = np.empty_like(x)
+    plan.execute_host(x, page_out)
+    assert np.array_equal(page_out, want)
+    if kind != 3:                                        # the radix-8 stage cannot run in place
+        plan.execute_host(pin_in, pin_in)
+        assert np.array_equal(pin_in.numpy(), want)
+
+
+def test_batch_execute_host_zero_copy(gb):
+    """Pinned buffers: one zero-copy persistent launch per storage type (the
+    radix-8 stage segment is copied through its device buffers); pageable
+    buffers: copies and the graph.  Ragged counts leave partial tiles."""
+    specs = [(2, 1024, 12289), (0, 256, 12289), (1, 64, 12289), (8, 4096, 12289), (5, 4096, 998244353),
+             (4, 8192, 998244353), (3, 512, 12289)]
+    rng = np.random.default_rng(SEED + 99)
+    plans, ins, d_in, d_out = [], [], [], []
+    for kind, n, q in specs:
+        dt = np.int32 if kind in (4, 5) else np.int16
+        plans.append(gb.Plan(kind, n, q, root_for(q, n)))
+        ins.append(rng.integers(0, q, (37 + 3 * len(ins), n)).astype(dt))
+        d_in.append(torch.from_numpy(ins[-1]).cuda())
+        d_out.append(torch.empty_like(d_in[-1]))
+    batch = gb.Batch([(plans[i], d_in[i], d_out[i]) for i in range(len(specs))])
+    batch.execute()
+    torch.cuda.synchronize()
+    want = [t.cpu().numpy() for t in d_out]
+    pin_in = [torch.from_numpy(x).pin_memory() for x in ins]
+    pin_out = [torch.empty_like(t).pin_memory() for t in pin_in]
+    c0 = gb.launch_count()
+    batch.execute_host(pin_in, pin_out)                  # zero copy: int16 + int32 launches, + r8 stage
+    assert gb.launch_count() - c0 == 3
+    assert all(np.array_equal(a.numpy(), b) for a, b in zip(pin_out, want))
+    batch.execute_host(pin_in, pin_in)                   # in place on the host buffers
+    assert all(np.array_equal(a.numpy(), b) for a, b in zip(pin_in, want))
+    page_out = [np.empty_like(x) for x in ins]
+    batch.execute_host(ins, page_out)                    # copies + one persistent launch
+    assert all(np.array_equal(a, b) for a, b in zip(page_out, want))
+
+
 # ---------------------------------------------------------------------------
 # fused bit reversal (natural order) and fused n^-1 epilogue
 # ---------------------------------------------------------------------------

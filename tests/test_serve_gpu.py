@@ -25,8 +25,12 @@ def _plans(gb):
         specs += [(0, n, 12289), (1, n, 12289)]
     for n, q in ((256, 998244353), (4096, 754974721), (65536, 469762049), (2048, 167772161)):
         specs += [(4, n, q), (5, n, q)]
-    specs.append((2, 1024, 12289))
-    return specs, [gb.Plan(k, n, q, root_for(q, n)) for k, n, q in specs]
+    specs += [(2, 1024, 12289), (9, 1024, 12289), (8, 512, 12289)]
+    plans = [gb.Plan(k, n, q, root_for(q, n)) for k, n, q in specs]
+    # output options travel with the plan: natural order + n^-1 scaling on an inverse
+    specs.append((1, 2048, 12289))
+    plans.append(gb.Plan(1, 2048, 12289, root_for(12289, 2048), 0, gb.FLAG_NATURAL_ORDER | gb.FLAG_SCALE_NINV))
+    return specs, plans
 
 
 def test_mix_equals_alone(gb):
@@ -84,4 +88,30 @@ def test_open_loop_schedule(gb):
     st = srv.stats()
     assert st["completed"] == n_req
     assert len(tickets) == n_req
+    srv.close()
+
+
+def test_pageable_and_pinned_requests(gb):
+    """Pageable buffers go through the copy engine, pinned ones through the
+    gather/scatter kernels; a micro-batch may mix both."""
+    specs, plans = _plans(gb)
+    srv = gb.Server(plans, slots=2)
+    rng = np.random.default_rng(77)
+    reqs = []
+    for k in range(120):
+        i = int(rng.integers(0, len(specs)))
+        kind, n, q = specs[i]
+        dt = np.int32 if kind in (4, 5) else np.int16
+        x = rng.integers(0, q, (2, n)).astype(dt)
+        if k % 2:
+            h_in, h_out = x, np.empty_like(x)
+        else:
+            h_in = torch.from_numpy(x).pin_memory()
+            h_out = torch.empty_like(h_in).pin_memory()
+        reqs.append((i, x, h_out, srv.submit(i, h_in, h_out)))
+    for _, _, _, t in reqs:
+        srv.wait(t, 60000)
+    for i, x, h_out, _ in reqs:
+        got = h_out if isinstance(h_out, np.ndarray) else h_out.numpy()
+        assert np.array_equal(plans[i](torch.from_numpy(x).cuda()).cpu().numpy(), got), specs[i]
     srv.close()
