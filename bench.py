@@ -323,7 +323,7 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "polys_per_step": polys,
                    "coefficients_per_step": sum(n * cnt for _, n, cnt, _ in SEGMENTS),
                    "algorithmic_bytes_per_step": algo_bytes, "launch": "one persistent kernel, CUDA graph replay",
-                   "autotuned_log2_coeffs_per_thread": batch.query(4),
+                   "autotuned_log2_coeffs_per_thread": batch.query(4), "autotuned_cta_threads": batch.query(6),
                    "l2": "flushed before every step (256 MiB write, untimed)", "parallelism": f"replicas{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src,

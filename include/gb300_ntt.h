@@ -180,6 +180,9 @@ int gbntt_batch_status(gbntt_batch* batch);
 #define GBNTT_BQ_SMEM     3   /* dynamic shared memory per CTA (bytes)   */
 #define GBNTT_BQ_EL16     4   /* log2 coefficients per thread chosen for the int16 launch */
 #define GBNTT_BQ_FAMSET   5   /* design families compiled into the chosen int16 kernel (bit mask) */
+#define GBNTT_BQ_CTA      6   /* threads per CTA of the chosen int16 kernel */
+/* Setting the environment variable GBNTT_TUNE_LOG=1 prints the autotuner's
+ * timing of every candidate configuration to stderr at batch creation. */
 int gbntt_batch_query(const gbntt_batch* batch, int what, int64_t* value);
 int gbntt_batch_destroy(gbntt_batch* batch);
 
@@ -208,11 +211,18 @@ int gbntt_batch_execute_noalloc(const gbntt_segment* segs, uint32_t nsegs, void*
  * may be submitted from any host thread.  A worker thread admits them while
  * the server's device arena has room (its size is the configured budget,
  * capped at half of the HBM free at creation), groups the waiting ones by
- * plan into a micro-batch per free stream slot (one in-place launch per plan
- * group), and overlaps the copies and kernels of up to `slots` micro-batches.
- * Host buffers should be pinned for the copies to overlap.  Requests larger
- * than the whole arena are refused (their wait returns GBNTT_ERR_ADMISSION).
- * Latency = submit to completion as seen by the worker. */
+ * plan into a micro-batch per free stream slot, and overlaps the copies and
+ * kernels of up to `slots` micro-batches.  A micro-batch is one in-place
+ * launch of the persistent kernel per storage type covering all its plan
+ * groups (int32 n >= 2^16 and the radix-4 inverse, bit-reversal and full
+ * Barrett designs: their plans' own launches).  Page-locked host buffers
+ * mapped into the device's address space are read and written by a gather and
+ * a scatter kernel (no per-request copy call); other host memory goes through
+ * one cudaMemcpyAsync per direction.  Both buffers of a request must stay
+ * valid and untouched until its wait returns.  Requests larger than the whole
+ * arena are refused (their wait returns GBNTT_ERR_ADMISSION).  Latency =
+ * submit to completion as seen by the worker.  Radix-8 stage plans (which
+ * cannot run in place) are rejected at creation. */
 typedef struct gbntt_server gbntt_server;
 typedef struct gbntt_server_config {
     uint32_t slots;                   /* concurrent micro-batches (streams); 0 = 4 */

@@ -11,9 +11,13 @@ constexpr int R4 = 1 << F_R4F16;
 constexpr int R8 = 1 << F_R8F16;
 constexpr int ALL16 = R2 | R4 | R8;
 
-#define GB_CFG(EL, SET) {false, EL, SET, reinterpret_cast<const void*>(&k_batch<false, BATCH_CTA, EL, SET>), nullptr}
+#define GB_CFG(EL, SET, CTA) \
+    {false, EL, SET, reinterpret_cast<const void*>(&k_batch<false, CTA, EL, SET>), nullptr, CTA}
+// 256-thread CTAs.  (768-thread CTAs, one per SM so that every warp of an SM
+// runs the same phase of the same tile, measured no faster on GB300.)
 BatchConfig kI16[] = {
-    GB_CFG(6, R4), GB_CFG(5, R4), GB_CFG(6, R2), GB_CFG(5, R2), GB_CFG(6, R8), GB_CFG(5, R8), GB_CFG(5, ALL16),
+    GB_CFG(6, R4, 256), GB_CFG(5, R4, 256), GB_CFG(6, R2, 256), GB_CFG(5, R2, 256), GB_CFG(6, R8, 256),
+    GB_CFG(5, R8, 256), GB_CFG(5, ALL16, 256),
 };
 #undef GB_CFG
 }  // namespace
@@ -22,7 +26,7 @@ int batch_configs_i16(const BatchConfig** out) {
     // the 32-coefficient configurations also carry the zero-copy form (batch_k16_zc.cu)
     static const bool linked = [] {
         for (auto& c : kI16)
-            if (c.elmax == 5) c.zfn = batch_zc_kernel_i16(c.set);
+            if (c.elmax == 5 && c.cta == BATCH_CTA) c.zfn = batch_zc_kernel_i16(c.set);
         return true;
     }();
     (void)linked;

@@ -24,10 +24,15 @@ constexpr int BATCH_CTA = 256;
     X(F_R2G32, 2) X(F_R2G32, 3) X(F_R2G32, 4) X(F_R2G32, 5) X(F_R2G32, 6) X(F_R2G32, 7) X(F_R2G32, 8)         \
     X(F_R2G32, 9) X(F_R2G32, 10) X(F_R2G32, 11) X(F_R2G32, 12) X(F_R2G32, 13)
 
+// resident CTAs per SM the register budget is sized for
+__host__ __device__ constexpr int batch_min_blocks(bool i32, int cta, int elmax) {
+    return cta >= 512 ? 1 : (i32 || elmax > 5) ? 2 : 3;
+}
+
 // SET: bit mask of the families whose variants this instantiation carries
 // (one kernel per family keeps the register allocation of one design).
 template <bool I32, int CTA, int ELMAX, int SET>
-__global__ void __launch_bounds__(CTA, (I32 || ELMAX > 5) ? 2 : 3) k_batch(const BatchDev b, int stage_bytes) {
+__global__ void __launch_bounds__(CTA, batch_min_blocks(I32, CTA, ELMAX)) k_batch(const BatchDev b, int stage_bytes) {
     extern __shared__ __align__(128) unsigned char bsmem[];
     unsigned long long* bar = reinterpret_cast<unsigned long long*>(bsmem);
     KArgs* ka = reinterpret_cast<KArgs*>(bsmem + 64);
@@ -56,6 +61,21 @@ __global__ void __launch_bounds__(CTA, (I32 || ELMAX > 5) ? 2 : 3) k_batch(const
         mbar_expect_tx(&bar[i], bytes);
         bulk_load(stage0 + i * stage_bytes, src, bytes, &bar[i]);
     };
+    // thread 0: L2 prefetch of the input of tile t (a hint; out-of-range t is ignored)
+    auto prefetch = [&](long long t) {
+        if (t >= total) return;
+        const SegDev* sd = &b.segs[seg_of(t)];
+        const long long lt = t - sd->tile0;
+        const long long P = sd->polys_per_tile;
+        const long long np = min(P, sd->a.batch - lt * P);
+        bulk_prefetch_l2(static_cast<const char*>(sd->a.in) + lt * P * sd->n * sd->elem_bytes,
+                         (unsigned)(np * sd->n * sd->elem_bytes));
+    };
+    // Tiles are handed out in increasing order, so tile t + PF_WAVES * gridDim.x
+    // is about PF_WAVES waves ahead of tile t: keeping that many waves of input
+    // requested from HBM hides its latency behind the transforms (the direct
+    // tile loads then mostly hit L2).
+    constexpr int PF_WAVES = 3;
 
     if (tid == 0) {
         mbar_init(&bar[0], 1);
@@ -70,6 +90,7 @@ __global__ void __launch_bounds__(CTA, (I32 || ELMAX > 5) ? 2 : 3) k_batch(const
             issue(t0, 0);
             sh_pending[0] = 1;
         }
+        for (int k = 1; k <= PF_WAVES; ++k) prefetch((long long)blockIdx.x + (long long)k * gridDim.x);
     }
     __syncthreads();
     long long t = sh_next;
@@ -87,6 +108,7 @@ __global__ void __launch_bounds__(CTA, (I32 || ELMAX > 5) ? 2 : 3) k_batch(const
                 bulk_wait_read();           // the other buffer's last store has left shared memory
                 issue(tn, buf ^ 1);
                 sh_pending[buf ^ 1] = 1;
+                prefetch(tn + (long long)PF_WAVES * gridDim.x);
             }
         }
         if (s != cur_seg) {
@@ -154,7 +176,7 @@ __global__ void __launch_bounds__(CTA, (I32 || ELMAX > 5) ? 2 : 3) k_batch(const
 // efficiently) instead of bulk copies, with one staging buffer per CTA; the
 // CTAs resident on an SM overlap one another's transfers.
 template <bool I32, int CTA, int ELMAX, int SET>
-__global__ void __launch_bounds__(CTA, (I32 || ELMAX > 5) ? 2 : 3) k_batch_zc(const BatchDev b, int stage_bytes) {
+__global__ void __launch_bounds__(CTA, batch_min_blocks(I32, CTA, ELMAX)) k_batch_zc(const BatchDev b, int stage_bytes) {
     extern __shared__ __align__(128) unsigned char bsmem[];
     KArgs* ka = reinterpret_cast<KArgs*>(bsmem + 64);
     unsigned char* stage = bsmem + SMEM_HEADER;
@@ -235,6 +257,7 @@ struct BatchConfig {
     int set;     // families covered (bit F)
     const void* fn;
     const void* zfn;   // zero-copy form (k_batch_zc), or nullptr
+    int cta;           // threads per CTA
 };
 
 // the configurations compiled into the library

@@ -115,7 +115,7 @@ extern "C" int gbntt_batch_execute_noalloc(const gbntt_segment* segs, uint32_t n
         const int ncfg = part ? batch_configs_i32(&cfgs) : batch_configs_i16(&cfgs);
         const BatchConfig* cfg = nullptr;
         for (int c = 0; c < ncfg && !cfg; ++c)
-            if (cfgs[c].elmax == 5 && (cfgs[c].set & fam_mask[part]) == fam_mask[part]) cfg = &cfgs[c];
+            if (cfgs[c].elmax == 5 && cfgs[c].cta == BATCH_CTA && (cfgs[c].set & fam_mask[part]) == fam_mask[part]) cfg = &cfgs[c];
         if (!cfg) return fail(GBNTT_ERR_ARG, "no persistent kernel covers these designs");
         // tiles, largest n first
         int order[GBNTT_NOALLOC_MAX_SEGMENTS];

@@ -518,7 +518,7 @@ int gbntt_server_create(gbntt_server** out, const gbntt_plan* const* plans, uint
             const int ncfg = p ? batch_configs_i32(&cfgs) : batch_configs_i16(&cfgs);
             const BatchConfig* cfg = nullptr;
             for (int c = 0; c < ncfg && !cfg; ++c)
-                if (cfgs[c].elmax == 5 && (cfgs[c].set & mask) == mask) cfg = &cfgs[c];
+                if (cfgs[c].elmax == 5 && cfgs[c].cta == BATCH_CTA && (cfgs[c].set & mask) == mask) cfg = &cfgs[c];
             if (!cfg) {   // no persistent kernel covers them: the plans launch on their own
                 for (auto& pi : s->pinfo)
                     if (pi.part == p) pi.part = -1;

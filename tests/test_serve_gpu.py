@@ -108,10 +108,13 @@ def test_pageable_and_pinned_requests(gb):
         else:
             h_in = torch.from_numpy(x).pin_memory()
             h_out = torch.empty_like(h_in).pin_memory()
-        reqs.append((i, x, h_out, srv.submit(i, h_in, h_out)))
-    for _, _, _, t in reqs:
+        # the caller keeps both buffers alive until the request completes: a
+        # freed pinned tensor goes back to torch's host cache and may be handed
+        # out again as another request's buffer while this one is in flight
+        reqs.append((i, x, h_in, h_out, srv.submit(i, h_in, h_out)))
+    for *_, t in reqs:
         srv.wait(t, 60000)
-    for i, x, h_out, _ in reqs:
+    for i, x, _, h_out, _ in reqs:
         got = h_out if isinstance(h_out, np.ndarray) else h_out.numpy()
         assert np.array_equal(plans[i](torch.from_numpy(x).cuda()).cpu().numpy(), got), specs[i]
     srv.close()
