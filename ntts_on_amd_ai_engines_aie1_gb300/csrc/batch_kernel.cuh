@@ -61,21 +61,6 @@ __global__ void __launch_bounds__(CTA, batch_min_blocks(I32, CTA, ELMAX)) k_batc
         mbar_expect_tx(&bar[i], bytes);
         bulk_load(stage0 + i * stage_bytes, src, bytes, &bar[i]);
     };
-    // thread 0: L2 prefetch of the input of tile t (a hint; out-of-range t is ignored)
-    auto prefetch = [&](long long t) {
-        if (t >= total) return;
-        const SegDev* sd = &b.segs[seg_of(t)];
-        const long long lt = t - sd->tile0;
-        const long long P = sd->polys_per_tile;
-        const long long np = min(P, sd->a.batch - lt * P);
-        bulk_prefetch_l2(static_cast<const char*>(sd->a.in) + lt * P * sd->n * sd->elem_bytes,
-                         (unsigned)(np * sd->n * sd->elem_bytes));
-    };
-    // Tiles are handed out in increasing order, so tile t + PF_WAVES * gridDim.x
-    // is about PF_WAVES waves ahead of tile t: keeping that many waves of input
-    // requested from HBM hides its latency behind the transforms (the direct
-    // tile loads then mostly hit L2).
-    constexpr int PF_WAVES = 3;
 
     if (tid == 0) {
         mbar_init(&bar[0], 1);
@@ -90,7 +75,6 @@ __global__ void __launch_bounds__(CTA, batch_min_blocks(I32, CTA, ELMAX)) k_batc
             issue(t0, 0);
             sh_pending[0] = 1;
         }
-        for (int k = 1; k <= PF_WAVES; ++k) prefetch((long long)blockIdx.x + (long long)k * gridDim.x);
     }
     __syncthreads();
     long long t = sh_next;
@@ -108,7 +92,6 @@ __global__ void __launch_bounds__(CTA, batch_min_blocks(I32, CTA, ELMAX)) k_batc
                 bulk_wait_read();           // the other buffer's last store has left shared memory
                 issue(tn, buf ^ 1);
                 sh_pending[buf ^ 1] = 1;
-                prefetch(tn + (long long)PF_WAVES * gridDim.x);
             }
         }
         if (s != cur_seg) {

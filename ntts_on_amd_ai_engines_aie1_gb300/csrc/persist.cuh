@@ -80,11 +80,6 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
     return false;
 }
 
-// hint: bring [src, src + bytes) into L2 (no completion to wait for)
-__device__ __forceinline__ void bulk_prefetch_l2(const void* src_gmem, unsigned bytes) {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src_gmem), "r"(bytes) : "memory");
-}
-
 __device__ __forceinline__ void bulk_load(void* dst_smem, const void* src_gmem, unsigned bytes,
                                           unsigned long long* bar) {
     asm volatile(
