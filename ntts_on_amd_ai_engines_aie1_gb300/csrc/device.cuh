@@ -596,7 +596,7 @@ __device__ __forceinline__ void store_poly(int (&v)[1 << EL], const KArgs& a, lo
 // ---------------------------------------------------------------------------
 
 template <int FAM, int L, int EL, int P, bool BR>
-__global__ void __launch_bounds__(P << (L - EL)) k_ntt(const __grid_constant__ KArgs a) {
+__device__ __forceinline__ void k_ntt_body(const KArgs& a) {
     constexpr int G = 1 << (L - EL);
     constexpr int NS = nsteps(FAM, L);
     constexpr int N = 1 << L;
@@ -635,6 +635,24 @@ __global__ void __launch_bounds__(P << (L - EL)) k_ntt(const __grid_constant__ K
     if (active) store_poly<I32, L, EL, LOZ>(v, a, poly, g);
 }
 
+// Two entry points over the same body.  Capping the int32 and radix-4 designs
+// at two resident 256-thread CTAs per SM (128 registers) raised their
+// throughput by up to a fifth on GB300; the same hint made the radix-2 and
+// radix-8 int16 code a fifth slower, so those keep the compiler's default.
+__host__ __device__ constexpr bool kntt_two_ctas(int fam, int threads) {
+    return threads <= 256 && (fam_i32(fam) || fam == F_R4F16);
+}
+
+template <int FAM, int L, int EL, int P, bool BR>
+__global__ void __launch_bounds__(P << (L - EL)) k_ntt(const __grid_constant__ KArgs a) {
+    k_ntt_body<FAM, L, EL, P, BR>(a);
+}
+
+template <int FAM, int L, int EL, int P, bool BR>
+__global__ void __launch_bounds__(P << (L - EL), 2) k_ntt2(const __grid_constant__ KArgs a) {
+    k_ntt_body<FAM, L, EL, P, BR>(a);
+}
+
 struct KernelInfo {
     const void* fn = nullptr;
     int threads = 0;
@@ -664,7 +682,10 @@ KernelInfo make_kernel_info() {
     constexpr int EL = choose_el(FAM, L);
     constexpr int P = choose_polys(FAM, L);
     KernelInfo ki;
-    ki.fn = reinterpret_cast<const void*>(&k_ntt<FAM, L, EL, P, BR>);
+    if constexpr (kntt_two_ctas(FAM, P << (L - EL)))
+        ki.fn = reinterpret_cast<const void*>(&k_ntt2<FAM, L, EL, P, BR>);
+    else
+        ki.fn = reinterpret_cast<const void*>(&k_ntt<FAM, L, EL, P, BR>);
     ki.threads = P << (L - EL);
     ki.smem = smem_bytes(FAM, L);
     ki.polys = P;
