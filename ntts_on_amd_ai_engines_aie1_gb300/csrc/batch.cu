@@ -181,11 +181,12 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
                 part.layouts.push_back(lay);
             }
         if (flags & GBNTT_BATCH_NO_TUNE) part.layouts.resize(1);   // the first (widest, most specific) one
-        for (int c = 0; c < ncfg; ++c)                              // zero copy: first covering configuration
-            if (cfgs[c].zfn && (cfgs[c].set & part.fam_mask) == part.fam_mask) {
+        // zero copy: the narrowest covering configuration (more CTAs per SM keep
+        // more tile transfers in flight on the host-device link)
+        for (int c = 0; c < ncfg; ++c)
+            if (cfgs[c].zfn && (cfgs[c].set & part.fam_mask) == part.fam_mask &&
+                (!part.zlay.cfg.zfn || cfgs[c].elmax < part.zlay.cfg.elmax))
                 part.zlay.cfg = cfgs[c];
-                break;
-            }
     }
     for (int i = 0; i < b->nparts; ++i) {
       auto& part = b->parts[i];

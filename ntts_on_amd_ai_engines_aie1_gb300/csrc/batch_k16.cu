@@ -1,9 +1,16 @@
-// batch_k16.cu -- persistent-kernel instantiations for the int16 designs:
-// one per family (radix-2 forward + inverse, radix-4, radix-8) and a generic
-// one, each with 32 and 64 coefficients per thread (the generic one: 32).
+// batch_k16.cu -- the configuration table of the int16 persistent kernels.
+// The kernels are instantiated in batch_k16_w64.cu, batch_k16_w32.cu,
+// batch_k16_w32g.cu, batch_k16_w16.cu and batch_k16_w16g.cu (compiled in
+// parallel); the zero-copy forms in batch_k16_zc.cu.
 #include "batch_kernel.cuh"
 
 namespace gbntt {
+
+const void* batch_kernels_i16_w64(int el, int set, int occ);
+const void* batch_kernels_i16_w32(int el, int set, int occ);
+const void* batch_kernels_i16_w32g(int el, int set, int occ);
+const void* batch_kernels_i16_w16(int el, int set, int occ);
+const void* batch_kernels_i16_w16g(int el, int set, int occ);
 
 namespace {
 constexpr int R2 = (1 << F_R2F16) | (1 << F_R2I16);
@@ -11,27 +18,37 @@ constexpr int R4 = 1 << F_R4F16;
 constexpr int R8 = 1 << F_R8F16;
 constexpr int ALL16 = R2 | R4 | R8;
 
-#define GB_CFG(EL, SET, CTA) \
-    {false, EL, SET, reinterpret_cast<const void*>(&k_batch<false, CTA, EL, SET>), nullptr, CTA}
-// 256-thread CTAs.  (768-thread CTAs, one per SM so that every warp of an SM
-// runs the same phase of the same tile, measured no faster on GB300.)
-BatchConfig kI16[] = {
-    GB_CFG(6, R4, 256), GB_CFG(5, R4, 256), GB_CFG(6, R2, 256), GB_CFG(5, R2, 256), GB_CFG(6, R8, 256),
-    GB_CFG(5, R8, 256), GB_CFG(5, ALL16, 256),
+struct Key {
+    int el, set, occ;
 };
-#undef GB_CFG
+// 256-thread CTAs with 64, 32 or 16 coefficients per thread; the narrower
+// ones carry less unrolled code per variant and fit more CTAs per SM (occ:
+// the residency the registers are budgeted for, 0 = the default of the width).
+// The order matters: GBNTT_BATCH_NO_TUNE takes the first covering entry.
+// (768-thread CTAs, one per SM, measured no faster on GB300.)
+constexpr Key kKeys[] = {
+    {6, R4, 0}, {5, R4, 0}, {6, R2, 0}, {5, R2, 0}, {6, R8, 0}, {5, R8, 0}, {5, ALL16, 0},
+    {4, R4, 0}, {4, R4, 5}, {4, R4, 6}, {4, R2, 0}, {4, R2, 5}, {4, R8, 0}, {4, ALL16, 0},
+};
+constexpr int kN = (int)(sizeof(kKeys) / sizeof(kKeys[0]));
+BatchConfig kI16[kN];
 }  // namespace
 
 int batch_configs_i16(const BatchConfig** out) {
-    // the 32-coefficient configurations also carry the zero-copy form (batch_k16_zc.cu)
-    static const bool linked = [] {
-        for (auto& c : kI16)
-            if (c.elmax == 5 && c.cta == BATCH_CTA) c.zfn = batch_zc_kernel_i16(c.set);
+    static const bool built = [] {
+        for (int i = 0; i < kN; ++i) {
+            const Key k = kKeys[i];
+            const void* fn = nullptr;
+            for (auto get : {batch_kernels_i16_w64, batch_kernels_i16_w32, batch_kernels_i16_w32g,
+                             batch_kernels_i16_w16, batch_kernels_i16_w16g})
+                if (!fn) fn = get(k.el, k.set, k.occ);
+            kI16[i] = BatchConfig{false, k.el, k.set, fn, batch_zc_kernel_i16(k.set, k.el), BATCH_CTA};
+        }
         return true;
     }();
-    (void)linked;
+    (void)built;
     *out = kI16;
-    return (int)(sizeof(kI16) / sizeof(kI16[0]));
+    return kN;
 }
 
 }  // namespace gbntt

@@ -26,13 +26,15 @@ constexpr int BATCH_CTA = 256;
 
 // resident CTAs per SM the register budget is sized for
 __host__ __device__ constexpr int batch_min_blocks(bool i32, int cta, int elmax) {
-    return cta >= 512 ? 1 : (i32 || elmax > 5) ? 2 : 3;
+    return cta >= 512 ? 1 : (i32 || elmax > 5) ? 2 : elmax == 5 ? 3 : 4;
 }
 
 // SET: bit mask of the families whose variants this instantiation carries
 // (one kernel per family keeps the register allocation of one design).
-template <bool I32, int CTA, int ELMAX, int SET>
-__global__ void __launch_bounds__(CTA, batch_min_blocks(I32, CTA, ELMAX)) k_batch(const BatchDev b, int stage_bytes) {
+// OCC: resident CTAs per SM the registers are budgeted for (0: batch_min_blocks)
+template <bool I32, int CTA, int ELMAX, int SET, int OCC = 0>
+__global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, ELMAX))
+    k_batch(const BatchDev b, int stage_bytes) {
     extern __shared__ __align__(128) unsigned char bsmem[];
     unsigned long long* bar = reinterpret_cast<unsigned long long*>(bsmem);
     KArgs* ka = reinterpret_cast<KArgs*>(bsmem + 64);
@@ -158,8 +160,9 @@ __global__ void __launch_bounds__(CTA, batch_min_blocks(I32, CTA, ELMAX)) k_batc
 // and stores (whole cache lines per warp, which the host-device link carries
 // efficiently) instead of bulk copies, with one staging buffer per CTA; the
 // CTAs resident on an SM overlap one another's transfers.
-template <bool I32, int CTA, int ELMAX, int SET>
-__global__ void __launch_bounds__(CTA, batch_min_blocks(I32, CTA, ELMAX)) k_batch_zc(const BatchDev b, int stage_bytes) {
+template <bool I32, int CTA, int ELMAX, int SET, int OCC = 0>
+__global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, ELMAX))
+    k_batch_zc(const BatchDev b, int stage_bytes) {
     extern __shared__ __align__(128) unsigned char bsmem[];
     KArgs* ka = reinterpret_cast<KArgs*>(bsmem + 64);
     unsigned char* stage = bsmem + SMEM_HEADER;
@@ -245,7 +248,7 @@ struct BatchConfig {
 
 // the configurations compiled into the library
 int batch_configs_i16(const BatchConfig** out);
-const void* batch_zc_kernel_i16(int set);   // k_batch_zc<int16, 32 coefficients per thread, set>
+const void* batch_zc_kernel_i16(int set, int elmax);   // k_batch_zc<int16, 2^elmax coefficients per thread, set>
 int batch_configs_i32(const BatchConfig** out);
 
 }  // namespace gbntt

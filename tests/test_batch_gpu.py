@@ -106,7 +106,7 @@ def test_batch_counts_launches(gb):
     torch.cuda.synchronize()
     assert gb.launch_count() == c0 + 1
     el = b.query(4)                       # coefficients per thread chosen by the autotuner
-    assert el in (5, 6)
+    assert el in (4, 5, 6)
     assert b.tiles == 4096 // (256 >> (10 - el))
     b2 = gb.Batch([(plan, x, y)], flags=1)   # autotuner off
     assert b2.query(4) == 6
