@@ -662,11 +662,16 @@ struct KernelInfo {
 };
 
 // elements per thread (log2) and polynomials per CTA of each design
+// Measured on GB300 (one box, same call): 16 coefficients per thread beat 32
+// and 64 for radix-2 int16 forward, radix-4, radix-8 and int32 up to n = 4096
+// (int32 n = 4096: 0.30 vs 0.43 vs 0.49 ms); 32 won for the radix-2 int16
+// inverse at n = 1024 and for int32 n = 2^14 (0.44 vs 0.50 vs 0.54 ms).  At
+// most 1024 threads per polynomial.
 __host__ __device__ constexpr int choose_el(int fam, int L) {
     if (L <= 5) return L;
-    if (fam == F_R4F16) return (L <= 8) ? 4 : 6;
-    if (fam == F_R8F16) return 6;
-    return L <= 12 ? (L + 1) / 2 : 6;
+    if (fam == F_R2I16) return L <= 12 ? (L + 1) / 2 : 6;
+    if (fam_i32(fam)) return L <= 12 ? 4 : (L - 10 > 5 ? L - 10 : 5);
+    return 4;
 }
 __host__ __device__ constexpr int choose_polys(int fam, int L) {
     const int G = 1 << (L - choose_el(fam, L));

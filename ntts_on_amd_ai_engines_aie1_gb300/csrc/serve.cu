@@ -504,7 +504,7 @@ int gbntt_server_create(gbntt_server** out, const gbntt_plan* const* plans, uint
         if (pi.fam >= 0 && variant_supported(pi.fam, pi.L)) pi.part = fam_i32(pi.fam) ? 1 : 0;
         s->pinfo.push_back(pi);
     }
-    // per storage type: the first 32-coefficient configuration covering the served families
+    // per storage type: one persistent configuration covering the served families
     {
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
@@ -516,9 +516,12 @@ int gbntt_server_create(gbntt_server** out, const gbntt_plan* const* plans, uint
             if (!mask) continue;
             const BatchConfig* cfgs = nullptr;
             const int ncfg = p ? batch_configs_i32(&cfgs) : batch_configs_i16(&cfgs);
+            // the narrowest covering configuration (16 coefficients per thread
+            // measured faster than 32 on mixed radix-4 batches)
             const BatchConfig* cfg = nullptr;
-            for (int c = 0; c < ncfg && !cfg; ++c)
-                if (cfgs[c].elmax == 5 && cfgs[c].cta == BATCH_CTA && (cfgs[c].set & mask) == mask) cfg = &cfgs[c];
+            for (int c = 0; c < ncfg; ++c)
+                if (cfgs[c].cta == BATCH_CTA && (cfgs[c].set & mask) == mask && (!cfg || cfgs[c].elmax < cfg->elmax))
+                    cfg = &cfgs[c];
             if (!cfg) {   // no persistent kernel covers them: the plans launch on their own
                 for (auto& pi : s->pinfo)
                     if (pi.part == p) pi.part = -1;
