@@ -363,13 +363,14 @@ def test_flags_in_a_batch(gb, orc):
         assert np.array_equal(y.cpu().numpy(), w), i
 
 
-@pytest.mark.parametrize("L", [16, 17, 19, 20])
+@pytest.mark.parametrize("L", [16, 17, 19, 20, 21, 22])
 @pytest.mark.parametrize("q", [998244353, 754974721])
 def test_r2_i32_two_pass(gb, orc, q, L):
-    """n = 2^16 .. 2^20: column pass + row pass, bit-exact with the reference's layers."""
+    """n = 2^16 .. 2^22: column pass + row pass, bit-exact with the reference's layers
+    (2^21 and 2^22: fewer columns per CTA in the column pass)."""
     n = 1 << L
     rng = np.random.default_rng(SEED + 1200 + L)
-    batch = 3 if L >= 19 else 5
+    batch = 1 if L >= 21 else 3 if L >= 19 else 5
     root = root_for(q, n)
     x = inputs(rng, batch, n, 0, q, np.int32)
     y = check(gb, orc, gb.Kind.R2_I32_FWD, orc.R2_I32_FWD, n, q, root, x)
