@@ -182,7 +182,9 @@ int gbntt_batch_status(gbntt_batch* batch);
 #define GBNTT_BQ_FAMSET   5   /* design families compiled into the chosen int16 kernel (bit mask) */
 #define GBNTT_BQ_CTA      6   /* threads per CTA of the chosen int16 kernel */
 /* Setting the environment variable GBNTT_TUNE_LOG=1 prints the autotuner's
- * timing of every candidate configuration to stderr at batch creation. */
+ * timing of every candidate configuration to stderr at batch creation;
+ * GBNTT_TUNE_FORCE="<log2 coefficients per thread>,<CTAs per SM, 0 = default>"
+ * pins the choice among the candidates (the timing launches still run). */
 int gbntt_batch_query(const gbntt_batch* batch, int what, int64_t* value);
 int gbntt_batch_destroy(gbntt_batch* batch);
 

@@ -112,13 +112,25 @@ int autotune(gbntt_batch* b) {
         size_t best = 0;
         for (size_t c = 1; c < p.layouts.size(); ++c)
             if (p.layouts[c].ms >= 0.f && p.layouts[c].ms < p.layouts[best].ms) best = c;
+        // GBNTT_TUNE_FORCE="<log2 coefficients per thread>,<CTAs per SM>" pins the
+        // choice (the timing launches still run), e.g. to profile the kernel a
+        // normal run picks while a profiler slows every launch down
+        if (const char* f = std::getenv("GBNTT_TUNE_FORCE")) {
+            int el = -1, occ = -1;
+            if (std::sscanf(f, "%d,%d", &el, &occ) == 2)
+                for (size_t c = 0; c < p.layouts.size(); ++c)
+                    if (p.layouts[c].cfg.elmax == el && p.layouts[c].cfg.occ == occ) {
+                        best = c;
+                        break;
+                    }
+        }
         p.chosen = (int)best;
         if (const char* log = std::getenv("GBNTT_TUNE_LOG"); log && *log == '1')
             for (size_t c = 0; c < p.layouts.size(); ++c)
-                std::fprintf(stderr, "gbntt autotune: %s part, %d coefficients/thread, %d threads/CTA, families 0x%x: "
-                             "%.2f us%s\n", p.i32 ? "int32" : "int16", 1 << p.layouts[c].cfg.elmax,
-                             p.layouts[c].cfg.cta, p.layouts[c].cfg.set, 1e3 * p.layouts[c].ms,
-                             c == best ? "  <- chosen" : "");
+                std::fprintf(stderr, "gbntt autotune: %s part, %d coefficients/thread, %d threads/CTA, %d CTAs/SM, "
+                             "families 0x%x: %.2f us%s\n", p.i32 ? "int32" : "int16", 1 << p.layouts[c].cfg.elmax,
+                             p.layouts[c].cfg.cta, p.layouts[c].cfg.occ, p.layouts[c].cfg.set,
+                             1e3 * p.layouts[c].ms, c == best ? "  <- chosen" : "");
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

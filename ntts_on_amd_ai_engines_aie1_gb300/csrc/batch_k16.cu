@@ -42,7 +42,7 @@ int batch_configs_i16(const BatchConfig** out) {
             for (auto get : {batch_kernels_i16_w64, batch_kernels_i16_w32, batch_kernels_i16_w32g,
                              batch_kernels_i16_w16, batch_kernels_i16_w16g})
                 if (!fn) fn = get(k.el, k.set, k.occ);
-            kI16[i] = BatchConfig{false, k.el, k.set, fn, batch_zc_kernel_i16(k.set, k.el), BATCH_CTA};
+            kI16[i] = BatchConfig{false, k.el, k.set, fn, batch_zc_kernel_i16(k.set, k.el), BATCH_CTA, k.occ};
         }
         return true;
     }();

@@ -7,7 +7,7 @@ namespace {
 constexpr int I32SET = (1 << F_R2F32) | (1 << F_R2G32);
 const BatchConfig kI32[] = {
     {true, 5, I32SET, reinterpret_cast<const void*>(&k_batch<true, BATCH_CTA, 5, I32SET>),
-     reinterpret_cast<const void*>(&k_batch_zc<true, BATCH_CTA, 5, I32SET>), BATCH_CTA},
+     reinterpret_cast<const void*>(&k_batch_zc<true, BATCH_CTA, 5, I32SET>), BATCH_CTA, 0},
 };
 }  // namespace
 

@@ -244,6 +244,7 @@ struct BatchConfig {
     const void* fn;
     const void* zfn;   // zero-copy form (k_batch_zc), or nullptr
     int cta;           // threads per CTA
+    int occ;           // resident CTAs per SM the registers are budgeted for (0: the default)
 };
 
 // the configurations compiled into the library
