@@ -108,6 +108,12 @@ __device__ __forceinline__ int hi16(int w) { return w >> 16; }
 // error is at most 0.5 + 0.75 and |result| <= 1.25 q < 2^15 for q < 2^16 / 3.
 __device__ __forceinline__ int br16(int a, int c, int q) { return a - rsz16(a * c) * q; }
 __device__ __forceinline__ int bm16(int a, int tw, int wq, int q) { return a * tw - rsz16(a * wq) * q; }
+// The same product when only its low 16 bits are used (it feeds sums that are
+// wrapped to int16): the packed table word t = (tw & 0xFFFF) | (w' << 16)
+// multiplies like tw modulo 2^16, so tw need not be sign-extended out of it.
+__device__ __forceinline__ unsigned bm16_lo(int a, int t, int q) {
+    return (unsigned)a * (unsigned)t - (unsigned)rsz16(a * hi16(t)) * (unsigned)q;
+}
 
 // int32 variants, computed modulo 2^32 like the int32 lanes
 __device__ __forceinline__ int br32(int a, int c, int q) {
@@ -353,9 +359,9 @@ __device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const
             const int blk = ((HIB ? (hi << L) : 0) | posmap<LO, EL>(g, k0)) >> (B + 1);
             if constexpr (FAM == F_R2F16) {
                 const int t = __ldg(&a.tab16[blk]);
-                const int u = br16(v[k0], a.c, q), w = bm16(v[k1], lo16(t), hi16(t), q);
-                v[k0] = wrap16(u + w);
-                v[k1] = wrap16(u - w);
+                const unsigned u = (unsigned)br16(v[k0], a.c, q), w = bm16_lo(v[k1], t, q);
+                v[k0] = wrap16((int)(u + w));
+                v[k1] = wrap16((int)(u - w));
             } else {
                 const int2 t = __ldg(&a.tab[blk]);
                 const int u = br32(v[k0], a.c, q), w = bm32(v[k1], t.x, t.y, q);
@@ -380,9 +386,9 @@ __device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const
             } else {
                 const int tpos = posmap<LO, EL>(g, k0) & ((1 << B) - 1);
                 const int t = __ldg(&a.tab16[(1 << B) + tpos]);
-                const int u = br16(v[k0], a.c, q), w = bm16(v[k1], lo16(t), hi16(t), q);
-                v[k0] = wrap16(u + w);
-                v[k1] = wrap16(u - w);
+                const unsigned u = (unsigned)br16(v[k0], a.c, q), w = bm16_lo(v[k1], t, q);
+                v[k0] = wrap16((int)(u + w));
+                v[k1] = wrap16((int)(u - w));
             }
         } else if constexpr (FAM == F_R4F16) {
             // radix-4 layer S (ntt_r4_kernels.cc:243-261)
@@ -391,26 +397,32 @@ __device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const
             // the multiplier of 1, read from table entry 0.
             constexpr int OFF = 4 * (((1 << (2 * S)) - 1) / 3);
             const int ka = k0, kb1 = k0 | (1 << KB), kb2 = k0 | (2 << KB), kb3 = k0 | (3 << KB);
-            int A0, A1, A2, A3;
+            // A0 always uses the multiplier of twiddle 1; A2 only feeds the
+            // wrapped sums, so it may keep bits above 16 (bm16_lo); A1 and A3
+            // are multiplied again by omega_4 and must be exact.
+            int A1, A3;
+            unsigned A2;
+            const int A0 = br16(v[ka], a.wq1, q);
             if constexpr (S == 0) {
-                A0 = br16(v[ka], a.wq1, q);
                 A1 = br16(v[kb1], a.wq1, q);
-                A2 = br16(v[kb2], a.wq1, q);
+                A2 = (unsigned)br16(v[kb2], a.wq1, q);
                 A3 = br16(v[kb3], a.wq1, q);
             } else {
                 const int blk = posmap<LO, EL>(g, k0) >> (B + 2);
                 const int4 t = __ldg(reinterpret_cast<const int4*>(a.tab16 + OFF + 4 * blk));
-                A0 = br16(v[ka], hi16(t.x), q);
                 A1 = bm16(v[kb1], lo16(t.y), hi16(t.y), q);
-                A2 = bm16(v[kb2], lo16(t.z), hi16(t.z), q);
+                A2 = bm16_lo(v[kb2], t.z, q);
                 A3 = bm16(v[kb3], lo16(t.w), hi16(t.w), q);
             }
             const int A5 = bm16(A1, a.fneg, a.wc, q);
             const int A6 = bm16(A3, a.fneg, a.wc, q);
-            v[ka] = wrap16(A0 + A1 + A2 + A3);
-            v[kb1] = wrap16(A0 - A1 + A2 - A3);    // y2 -> digit bitrev2(2) = 1
-            v[kb2] = wrap16(A0 + A5 - A2 - A6);    // y1 -> digit 2
-            v[kb3] = wrap16(A0 - A5 - A2 + A6);    // y3 -> digit 3
+            const unsigned s02 = (unsigned)A0 + A2, d02 = (unsigned)A0 - A2;
+            const unsigned s13 = (unsigned)A1 + (unsigned)A3, d13 = (unsigned)A1 - (unsigned)A3;
+            const unsigned d56 = (unsigned)A5 - (unsigned)A6;
+            v[ka] = wrap16((int)(s02 + s13));      // y0
+            v[kb1] = wrap16((int)(s02 - s13));     // y2 -> digit bitrev2(2) = 1
+            v[kb2] = wrap16((int)(d02 + d56));     // y1 -> digit 2
+            v[kb3] = wrap16((int)(d02 - d56));     // y3 -> digit 3
         } else if constexpr (FAM == F_R8F16) {
             if constexpr (W == 3) {
                 // radix-8 stage S: y = x F8 (int32), then the reduction tile

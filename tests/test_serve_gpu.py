@@ -38,14 +38,16 @@ def test_mix_equals_alone(gb):
     srv = gb.Server(plans, slots=4, device_bytes=64 << 20, max_requests_per_batch=64)
     rng = np.random.default_rng(123)
     reqs = []
-    for _ in range(300):
+    for _ in range(300):                              # buffers first, then one burst of submissions
         i = int(rng.integers(0, len(specs)))
         kind, n, q = specs[i]
         dt = np.int32 if kind in (4, 5) else np.int16
         cnt = int(rng.integers(1, 4))
         h_in = torch.from_numpy(rng.integers(0, q, (cnt, n)).astype(dt)).pin_memory()
-        h_out = torch.empty_like(h_in).pin_memory()
-        reqs.append((i, h_in, h_out, srv.submit(i, h_in, h_out)))
+        reqs.append((i, h_in, torch.empty_like(h_in).pin_memory()))
+    tickets = srv.submit_schedule([r[0] for r in reqs], [r[1] for r in reqs], [r[2] for r in reqs],
+                                  [r[1].shape[0] for r in reqs], [0.0] * len(reqs))
+    reqs = [r + (t,) for r, t in zip(reqs, tickets)]
     for _, _, _, t in reqs:
         srv.wait(t, 60000)
     st = srv.stats()
