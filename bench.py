@@ -38,6 +38,29 @@ WORKLOAD = ("batched radix-4 int16 forward NTT: 4096 polys x 4 moduli {7681,1075
             "n=256 for 7681/10753 (no 1024-th root of unity), n=1024 for 12289")
 
 
+def workload_config():
+    """The workload part of the JSON line's config, shared by both arms."""
+    return {"workload": WORKLOAD, "polys_per_step": sum(cnt for _, _, cnt, _ in SEGMENTS),
+            "coefficients_per_step": sum(n * cnt for _, n, cnt, _ in SEGMENTS),
+            "algorithmic_bytes_per_step": sum(2 * n * 2 * cnt for _, n, cnt, _ in SEGMENTS)}
+
+
+def max_over_ranks(x, dist=None, device="cpu"):
+    """The slowest rank's value (every rank calls it; `dist` None on one process)."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_value(polys_per_rank, world, ms_max):
+    """Replicas: every rank transforms its own copy of the batch; the job's
+    throughput is all ranks' polynomials over the slowest rank's step time."""
+    return world * polys_per_rank / (ms_max / 1e3)
+
+
 def root_of(q, n, g):
     if q == 12289:
         return pow(41, 4096 // n, q)
@@ -172,7 +195,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "NTT/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int16", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "polys_per_step": per_step},
+        "config": {**workload_config(), "parallelism": f"replicas{args.gpus}",
+                   "sampled_polys_per_step": per_step},
         "cpu_baseline": {"value": value, "unit": "NTT/s", "cores": threads, "kind": "port",
                          "sample": desc + "; the reference's AIE kernels cannot be built here, so its CPU "
                                           "restatement (oracle/ntt_oracle.c, the parity oracle) is timed"},
@@ -242,12 +266,8 @@ def run_ours(args):
         dist.barrier()
     sampler.stop()
     batch.status()
-    ms = sum(step_ms) / len(step_ms)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * polys / (ms / 1e3)
+    ms = max_over_ranks(sum(step_ms) / len(step_ms), dist, dev)
+    value = whole_job_value(polys, world, ms)
     peak, peak_src = load_peaks()
     achieved = algo_bytes / (ms / 1e3) / 1e9
     traffic = load_traffic()
@@ -320,9 +340,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "NTT/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int16", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "polys_per_step": polys,
-                   "coefficients_per_step": sum(n * cnt for _, n, cnt, _ in SEGMENTS),
-                   "algorithmic_bytes_per_step": algo_bytes, "launch": "one persistent kernel, CUDA graph replay",
+        "config": {**workload_config(), "launch": "one persistent kernel, CUDA graph replay",
                    "autotuned_log2_coeffs_per_thread": batch.query(4), "autotuned_cta_threads": batch.query(6),
                    "l2": "flushed before every step (256 MiB write, untimed)", "parallelism": f"replicas{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

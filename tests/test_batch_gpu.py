@@ -110,3 +110,19 @@ def test_batch_counts_launches(gb):
     assert b.tiles == 4096 // (256 >> (10 - el))
     b2 = gb.Batch([(plan, x, y)], flags=1)   # autotuner off
     assert b2.query(4) == 6
+
+
+def test_autotune_force(gb, monkeypatch):
+    """GBNTT_TUNE_FORCE pins the autotuner's choice (used for reproducible profiles)."""
+    plan = gb.Plan(2, 1024, 12289, root_for(12289, 1024))
+    x = torch.randint(0, 12289, (512, 1024), dtype=torch.int16, device="cuda")
+    y = torch.empty_like(x)
+    want = plan(x)
+    for el in (6, 5, 4):
+        monkeypatch.setenv("GBNTT_TUNE_FORCE", f"{el},0")
+        b = gb.Batch([(plan, x, y)])
+        assert b.query(4) == el and b.query(6) == 256
+        y.zero_()
+        b.graph_launch()
+        torch.cuda.synchronize()
+        assert torch.equal(y, want)
