@@ -252,7 +252,12 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
                 gbntt_batch_destroy(b);
                 return batch_fail(GBNTT_ERR_CUDA, std::string("batch kernel configuration: ") + cudaGetErrorString(e));
             }
-            lay.grid = (int)std::min<long long>((long long)per_sm * sms, lay.total_tiles);
+            // Zero copy: two CTAs per SM.  The link, not the SMs, is the limit;
+            // fewer tiles in flight shorten the read-only start and the
+            // write-only end of the launch (benchmark batch end to end: 1, 2, 3,
+            // 4 CTAs/SM -> 100, 106, 103, 100 M NTT/s on one box).
+            const int resident = zc ? std::min(per_sm, 2) : per_sm;
+            lay.grid = (int)std::min<long long>((long long)resident * sms, lay.total_tiles);
             e = cudaMalloc(&lay.d_segs, sizeof(SegDev) * lay.segs.size());
             if (e == cudaSuccess)
                 e = cudaMemcpy(lay.d_segs, lay.segs.data(), sizeof(SegDev) * lay.segs.size(), cudaMemcpyHostToDevice);
