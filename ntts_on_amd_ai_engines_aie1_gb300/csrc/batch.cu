@@ -182,22 +182,26 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
         part.pending.push_back({k, fam, L, eb, a});
     }
     // candidate configurations of each part: those whose family set covers it
+    // and whose CTAs hold its longest transform
     for (int i = 0; i < b->nparts; ++i) {
         auto& part = b->parts[i];
+        int maxL = 0;
+        for (const auto& pe : part.pending) maxL = std::max(maxL, pe.L);
         const BatchConfig* cfgs = nullptr;
         const int ncfg = part.i32 ? batch_configs_i32(&cfgs) : batch_configs_i16(&cfgs);
+        auto covers = [&](const BatchConfig& c) {
+            return (c.set & part.fam_mask) == part.fam_mask && config_fits(c, maxL);
+        };
         for (int c = 0; c < ncfg; ++c)
-            if ((cfgs[c].set & part.fam_mask) == part.fam_mask) {
+            if (covers(cfgs[c])) {
                 gbntt_batch::Layout lay;
                 lay.cfg = cfgs[c];
                 part.layouts.push_back(lay);
             }
         if (flags & GBNTT_BATCH_NO_TUNE) part.layouts.resize(1);   // the first (widest, most specific) one
-        // zero copy: the narrowest covering configuration (more CTAs per SM keep
-        // more tile transfers in flight on the host-device link)
+        // zero copy: the narrowest covering configuration
         for (int c = 0; c < ncfg; ++c)
-            if (cfgs[c].zfn && (cfgs[c].set & part.fam_mask) == part.fam_mask &&
-                (!part.zlay.cfg.zfn || cfgs[c].elmax < part.zlay.cfg.elmax))
+            if (cfgs[c].zfn && covers(cfgs[c]) && (!part.zlay.cfg.zfn || cfgs[c].elmax < part.zlay.cfg.elmax))
                 part.zlay.cfg = cfgs[c];
     }
     for (int i = 0; i < b->nparts; ++i) {

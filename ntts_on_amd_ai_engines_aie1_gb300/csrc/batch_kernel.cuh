@@ -24,6 +24,11 @@ constexpr int BATCH_CTA = 256;
     X(F_R2G32, 2) X(F_R2G32, 3) X(F_R2G32, 4) X(F_R2G32, 5) X(F_R2G32, 6) X(F_R2G32, 7) X(F_R2G32, 8)         \
     X(F_R2G32, 9) X(F_R2G32, 10) X(F_R2G32, 11) X(F_R2G32, 12) X(F_R2G32, 13)
 
+// a polynomial of 2^L coefficients fits one CTA of `cta` threads at 2^elmax per thread
+__host__ __device__ constexpr bool batch_fits(int L, int cta, int elmax) {
+    return (1 << (L - (L < elmax ? L : elmax))) <= cta;
+}
+
 // resident CTAs per SM the register budget is sized for
 __host__ __device__ constexpr int batch_min_blocks(bool i32, int cta, int elmax) {
     return cta >= 512 ? 1 : (i32 || elmax > 5) ? 2 : elmax == 5 ? 3 : 4;
@@ -115,7 +120,8 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
         switch (variant) {
 #define GB_CASE(F, L)                                                     \
     case variant_id(F, L):                                                \
-        if constexpr (fam_i32(F) == I32 && ((SET >> F) & 1)) tile_transform<F, L, CTA, ELMAX>(st, xbuf, kc, *ka, np); \
+        if constexpr (fam_i32(F) == I32 && ((SET >> F) & 1) && batch_fits(L, CTA, ELMAX))            \
+            tile_transform<F, L, CTA, ELMAX>(st, xbuf, kc, *ka, np);                                       \
         break;
             GB_I16_VARIANTS(GB_CASE)
             GB_I32_VARIANTS(GB_CASE)
@@ -204,7 +210,8 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
         switch (sd->variant) {
 #define GB_CASE(F, L)                                                     \
     case variant_id(F, L):                                                \
-        if constexpr (fam_i32(F) == I32 && ((SET >> F) & 1)) tile_transform<F, L, CTA, ELMAX>(stage, xbuf, kc, *ka, np); \
+        if constexpr (fam_i32(F) == I32 && ((SET >> F) & 1) && batch_fits(L, CTA, ELMAX))            \
+            tile_transform<F, L, CTA, ELMAX>(stage, xbuf, kc, *ka, np);                                    \
         break;
             GB_I16_VARIANTS(GB_CASE)
             GB_I32_VARIANTS(GB_CASE)
@@ -246,6 +253,9 @@ struct BatchConfig {
     int cta;           // threads per CTA
     int occ;           // resident CTAs per SM the registers are budgeted for (0: the default)
 };
+
+// the configuration carries a transform of 2^L coefficients
+inline bool config_fits(const BatchConfig& c, int L) { return batch_fits(L, c.cta, c.elmax); }
 
 // the configurations compiled into the library
 int batch_configs_i16(const BatchConfig** out);

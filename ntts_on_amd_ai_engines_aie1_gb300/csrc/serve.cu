@@ -510,9 +510,12 @@ int gbntt_server_create(gbntt_server** out, const gbntt_plan* const* plans, uint
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         for (int p = 0; p < 2; ++p) {
-            int mask = 0, stage = 0, xbytes = 0;
+            int mask = 0, stage = 0, xbytes = 0, maxL = 0;
             for (const auto& pi : s->pinfo)
-                if (pi.part == p) mask |= 1 << pi.fam;
+                if (pi.part == p) {
+                    mask |= 1 << pi.fam;
+                    maxL = std::max(maxL, pi.L);
+                }
             if (!mask) continue;
             const BatchConfig* cfgs = nullptr;
             const int ncfg = p ? batch_configs_i32(&cfgs) : batch_configs_i16(&cfgs);
@@ -520,7 +523,8 @@ int gbntt_server_create(gbntt_server** out, const gbntt_plan* const* plans, uint
             // measured faster than 32 on mixed radix-4 batches)
             const BatchConfig* cfg = nullptr;
             for (int c = 0; c < ncfg; ++c)
-                if (cfgs[c].cta == BATCH_CTA && (cfgs[c].set & mask) == mask && (!cfg || cfgs[c].elmax < cfg->elmax))
+                if (cfgs[c].cta == BATCH_CTA && (cfgs[c].set & mask) == mask && config_fits(cfgs[c], maxL) &&
+                    (!cfg || cfgs[c].elmax < cfg->elmax))
                     cfg = &cfgs[c];
             if (!cfg) {   // no persistent kernel covers them: the plans launch on their own
                 for (auto& pi : s->pinfo)

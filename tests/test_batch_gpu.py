@@ -126,3 +126,25 @@ def test_autotune_force(gb, monkeypatch):
         b.graph_launch()
         torch.cuda.synchronize()
         assert torch.equal(y, want)
+
+
+@pytest.mark.parametrize("Ls", [(12, 8, 2), (13, 12, 5)])
+def test_int32_batch_widths(gb, monkeypatch, Ls):
+    """int32 batches: 16 coefficients per thread carry n <= 2^12; a batch with
+    n = 2^13 must keep to the 32-coefficient kernel, even when 16 is requested."""
+    monkeypatch.setenv("GBNTT_TUNE_FORCE", "4,0")
+    q = 998244353
+    rng = np.random.default_rng(5 + Ls[0])
+    segs, wants = [], []
+    for i, L in enumerate(Ls):
+        n = 1 << L
+        kind = 4 if i % 2 == 0 else 5
+        plan = gb.Plan(kind, n, q, root_for(q, n))
+        x = torch.from_numpy(rng.integers(0, q, (37, n)).astype(np.int32)).cuda()
+        segs.append((plan, x, torch.empty_like(x)))
+        wants.append(plan(x))
+    b = gb.Batch(segs)
+    b.execute()
+    torch.cuda.synchronize()
+    for (_, _, y), w in zip(segs, wants):
+        assert torch.equal(y, w)
