@@ -106,9 +106,15 @@ int gbntt_plan_destroy(gbntt_plan* plan);
 int gbntt_execute(const gbntt_plan* plan, const void* d_in, void* d_out, uint64_t batch,
                   void* stream);
 
-/* Same, on host buffers: copies the inputs to device staging memory owned by
- * the plan, transforms, copies back and waits for the stream.  Pinned host
- * buffers give full copy bandwidth.  Serialised per plan. */
+/* Same, on host buffers, and waits for the stream; serialised per plan.  When
+ * both buffers are page-locked and mapped into the device's address space
+ * (cudaHostAlloc / cudaHostRegister memory, 16-byte aligned) and the design
+ * has a persistent-kernel form (all but the radix-4 inverse, the radix-8
+ * stage, the bit-reversal and full Barrett units and int32 n >= 2^16), the
+ * zero-copy persistent kernel reads and writes them directly over the
+ * host-device link; its scratch (a descriptor and tile counters) is allocated
+ * on the first such call.  Otherwise the inputs are copied to device staging
+ * memory owned by the plan, transformed and copied back. */
 int gbntt_execute_host(gbntt_plan* plan, const void* h_in, void* h_out, uint64_t batch,
                        void* stream);
 

@@ -31,6 +31,7 @@ struct gbntt_plan {
     std::mutex stage_mu;   // serialises gbntt_execute_host on this plan
     void* d_stage = nullptr;
     size_t stage_bytes = 0;
+    void* zc_state = nullptr;   // zero-copy scratch (batch.cu), created on first use
 };
 
 namespace {
@@ -317,6 +318,7 @@ int gbntt_plan_destroy(gbntt_plan* p) {
     if (!p) return GBNTT_OK;
     if (p->d_tab) cudaFree(p->d_tab);
     if (p->d_stage) cudaFree(p->d_stage);
+    if (p->zc_state) gbntt_internal_zc_free(p->zc_state);
     delete p;
     return GBNTT_OK;
 }
@@ -351,11 +353,26 @@ int gbntt_execute_host(gbntt_plan* p, const void* h_in, void* h_out, uint64_t ba
     if (batch == 0) return GBNTT_OK;
     if (!h_in || !h_out) return fail(GBNTT_ERR_ARG, "null buffer");
     std::lock_guard<std::mutex> lock(p->stage_mu);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    {
+        // page-locked, mapped host buffers: the zero-copy persistent kernel reads
+        // and writes them directly, both directions of the link at once
+        const void* mi = gbntt_internal_mapped(h_in);
+        const void* mo = gbntt_internal_mapped(h_out);
+        if (mi && mo && !((reinterpret_cast<uintptr_t>(mi) | reinterpret_cast<uintptr_t>(mo)) & 15) &&
+            !(p->hp.kind == K_R8_I16_STAGE && h_in == h_out)) {
+            const int rc = gbntt_internal_zc_plan(&p->zc_state, p, mi, const_cast<void*>(mo), batch, s);
+            if (rc == GBNTT_OK) {
+                const cudaError_t e = cudaStreamSynchronize(s);
+                return e == cudaSuccess ? GBNTT_OK : cuda_fail(e, "cudaStreamSynchronize");
+            }
+            if (rc != GBNTT_ERR_KIND) return rc;
+        }
+    }
     const size_t bytes = (size_t)batch * p->hp.n * (size_t)p->hp.elem_bytes;
     // the radix-8 stage reads other threads' outputs, so it gets its own output half
     const bool split = (p->hp.kind == K_R8_I16_STAGE);
     const size_t need = split ? 2 * bytes : bytes;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaError_t e;
     if (p->stage_bytes < need) {
         if (p->d_stage) cudaFree(p->d_stage);

@@ -138,7 +138,89 @@ int autotune(gbntt_batch* b) {
     return rc;
 }
 
+// zero-copy scratch of one plan (gbntt_execute_host on mapped host buffers)
+struct ZcPlanState {
+    bool tried = false, usable = false;
+    BatchConfig cfg{};
+    int stage = 0, smem = 0, grid_cap = 0;
+    SegDev* d_seg = nullptr;
+    unsigned long long* d_ctr = nullptr;
+};
+
 }  // namespace
+
+int gbntt_internal_zc_plan(void** state, const gbntt_plan* p, const void* m_in, void* m_out, uint64_t count,
+                           cudaStream_t s) {
+    if (!count) return GBNTT_OK;
+    int fam, L, eb;
+    KArgs a;
+    gbntt_internal_plan_args(p, &fam, &L, &eb, &a);
+    if (fam < 0 || !variant_supported(fam, L)) return GBNTT_ERR_KIND;
+    if (!*state) *state = new ZcPlanState();
+    ZcPlanState& st = *static_cast<ZcPlanState*>(*state);
+    if (!st.tried) {
+        st.tried = true;
+        const bool i32 = fam_i32(fam);
+        const BatchConfig* cfgs = nullptr;
+        const int ncfg = i32 ? batch_configs_i32(&cfgs) : batch_configs_i16(&cfgs);
+        const BatchConfig* cfg = nullptr;   // the narrowest covering configuration with a zero-copy kernel
+        for (int c = 0; c < ncfg; ++c)
+            if (cfgs[c].zfn && ((cfgs[c].set >> fam) & 1) && config_fits(cfgs[c], L) &&
+                (!cfg || cfgs[c].elmax < cfg->elmax))
+                cfg = &cfgs[c];
+        if (!cfg) return GBNTT_ERR_KIND;
+        st.cfg = *cfg;
+        st.stage = (batch_stage_bytes(cfg->cta, L, eb, cfg->elmax) + 127) & ~127;
+        st.smem = SMEM_HEADER + st.stage + batch_xbuf_bytes(cfg->cta, L, cfg->elmax);
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaError_t e = cudaFuncSetAttribute(cfg->zfn, cudaFuncAttributeMaxDynamicSharedMemorySize, st.smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cfg->zfn, cfg->cta, st.smem);
+        if (e != cudaSuccess || per_sm < 1)
+            return batch_fail(GBNTT_ERR_CUDA, std::string("zero-copy kernel configuration: ") + cudaGetErrorString(e));
+        st.grid_cap = std::min(per_sm, 2) * sms;   // two CTAs per SM, as for batches
+        e = cudaMalloc(&st.d_seg, sizeof(SegDev));
+        if (e == cudaSuccess) e = cudaMalloc(&st.d_ctr, sizeof(unsigned long long) * CTR_WORDS);
+        if (e == cudaSuccess) e = cudaMemset(st.d_ctr, 0, sizeof(unsigned long long) * CTR_WORDS);
+        if (e != cudaSuccess) return batch_fail(GBNTT_ERR_NOMEM, "zero-copy scratch allocation failed");
+        st.usable = true;
+    }
+    if (!st.usable) return GBNTT_ERR_KIND;
+    SegDev sd;
+    std::memset(&sd, 0, sizeof(sd));
+    sd.a = a;
+    sd.a.in = m_in;
+    sd.a.out = m_out;
+    sd.a.batch = (long long)count;
+    sd.n = 1 << L;
+    sd.elem_bytes = eb;
+    sd.variant = variant_id(fam, L);
+    sd.polys_per_tile = st.cfg.cta >> (L - batch_el(L, st.cfg.elmax));
+    sd.tiles = ((long long)count + sd.polys_per_tile - 1) / sd.polys_per_tile;
+    cudaError_t e = cudaMemcpyAsync(st.d_seg, &sd, sizeof(SegDev), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("descriptor: ") + cudaGetErrorString(e));
+    BatchDev bd;
+    bd.segs = st.d_seg;
+    bd.nsegs = 1;
+    bd.total_tiles = sd.tiles;
+    bd.ctr = st.d_ctr;
+    int sb = st.stage;
+    void* args[] = {&bd, &sb};
+    const unsigned grid = (unsigned)std::min<long long>(st.grid_cap, sd.tiles);
+    e = cudaLaunchKernel(st.cfg.zfn, dim3(grid), dim3(st.cfg.cta), args, st.smem, s);
+    if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("zero-copy launch: ") + cudaGetErrorString(e));
+    gbntt_internal_count_launch();
+    return GBNTT_OK;
+}
+
+void gbntt_internal_zc_free(void* state) {
+    ZcPlanState* st = static_cast<ZcPlanState*>(state);
+    if (!st) return;
+    if (st->d_seg) cudaFree(st->d_seg);
+    if (st->d_ctr) cudaFree(st->d_ctr);
+    delete st;
+}
 
 extern "C" {
 

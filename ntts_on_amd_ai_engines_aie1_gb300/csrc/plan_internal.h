@@ -18,3 +18,11 @@ void gbntt_internal_plan_args(const gbntt_plan* p, int* fam, int* L, int* elem_b
 // can be read and written by the transform kernels directly over the
 // host-device link (zero copy).
 const void* gbntt_internal_mapped(const void* h);
+// Zero-copy execution of one plan on mapped host buffers through the zero-copy
+// persistent kernel (batch.cu).  `state` is the plan's scratch (descriptor and
+// tile counters, created on first use; freed with gbntt_internal_zc_free).
+// Returns GBNTT_ERR_KIND when no zero-copy kernel carries the design (the
+// caller then copies through device staging memory).
+int gbntt_internal_zc_plan(void** state, const gbntt_plan* p, const void* m_in, void* m_out, uint64_t count,
+                           cudaStream_t s);
+void gbntt_internal_zc_free(void* state);
