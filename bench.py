@@ -531,7 +531,7 @@ def run_serving(gb, seconds):
             nbytes += 2 * (1 << key[2]) * (key[0] // 8)
         return idx, ins, outl, nbytes
 
-    srv = gb.Server(plans, slots=4)
+    srv = gb.Server(plans, slots=8)
     # alone-vs-mix: a mixed burst with distinct output buffers, each checked against a lone launch
     idx, ins, _, _ = draw(256)
     own = [torch.empty_like(x).pin_memory() for x in ins]
@@ -557,7 +557,7 @@ def run_serving(gb, seconds):
     cap = nsat / el
     out = {"workload": "single-polynomial requests: n=2^U, U~{8..16} (int16: {8..12}), fwd/inv 50/50, "
                        "int16 q=12289 / int32 q in {998244353,469762049,167772161,754974721} 50/50",
-           "plans": len(plans), "slots": 4, "api": "gbntt_server_* (pinned host buffers)",
+           "plans": len(plans), "slots": 8, "api": "gbntt_server_* (pinned host buffers)",
            "alone_vs_mix_checked": 256,
            "saturation": {"requests_per_s": cap, "NTT_per_s": cap, "algorithmic_GBps": nbytes / el / 1e9,
                           "requests": nsat, "microbatches": st["microbatches"], "launches": st["launches"],

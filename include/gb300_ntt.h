@@ -233,7 +233,7 @@ int gbntt_batch_execute_noalloc(const gbntt_segment* segs, uint32_t nsegs, void*
  * cannot run in place) are rejected at creation. */
 typedef struct gbntt_server gbntt_server;
 typedef struct gbntt_server_config {
-    uint32_t slots;                   /* concurrent micro-batches (streams); 0 = 4 */
+    uint32_t slots;                   /* concurrent micro-batches (streams); 0 = 8 */
     uint32_t max_requests_per_batch;  /* 0 = 4096                                  */
     uint64_t device_bytes;            /* arena budget; 0 = 1 GiB                   */
 } gbntt_server_config;

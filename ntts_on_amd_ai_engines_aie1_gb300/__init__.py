@@ -291,7 +291,7 @@ def _hptr(a):
 class Server:
     """Continuous-batching request server over a fixed list of plans."""
 
-    def __init__(self, plans, slots=4, device_bytes=0, max_requests_per_batch=0):
+    def __init__(self, plans, slots=8, device_bytes=0, max_requests_per_batch=0):
         self.plans = list(plans)
         arr = (ctypes.c_void_p * len(self.plans))(*[p.handle for p in self.plans])
         cfg = ServerConfig(slots, max_requests_per_batch, device_bytes)

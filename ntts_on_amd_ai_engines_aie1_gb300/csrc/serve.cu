@@ -550,7 +550,8 @@ int gbntt_server_create(gbntt_server** out, const gbntt_plan* const* plans, uint
             pc.grid = per_sm * sms;
         }
     }
-    const uint32_t nslots = cfg && cfg->slots ? cfg->slots : 4;
+    // 8 slots: C5 mix at half load p50/p99 164/333 us vs 201/480 us with 4 (16: 156/311, less capacity)
+    const uint32_t nslots = cfg && cfg->slots ? cfg->slots : 8;
     s->max_group_requests = cfg && cfg->max_requests_per_batch ? cfg->max_requests_per_batch : 4096;
     cudaGetDevice(&s->device);
     size_t free_b = 0, total_b = 0;
