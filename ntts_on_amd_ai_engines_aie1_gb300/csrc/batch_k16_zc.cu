@@ -1,6 +1,6 @@
 // batch_k16_zc.cu -- zero-copy persistent-kernel instantiations for the int16
-// designs (32 coefficients per thread; radix-4 also 16), in their own
-// translation unit so they compile in parallel with batch_k16.cu.
+// designs (32 coefficients per thread for every family set, 16 for radix-4),
+// in their own translation unit so they compile in parallel.
 #include "batch_kernel.cuh"
 
 namespace gbntt {

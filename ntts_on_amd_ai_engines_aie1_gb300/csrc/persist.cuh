@@ -11,9 +11,10 @@
 //   shared buffer and leave with cp.async.bulk shared->global.
 //
 // Inside a tile every polynomial is transformed by the window/exchange scheme
-// of device.cuh with 32 coefficients per thread: with that width, the padded
-// exchange layout (one spare word per 32) is free of bank conflicts for every
-// window, and the strided staging layout is conflict-free as well.
+// of device.cuh with 16, 32 or 64 coefficients per thread (the configuration's
+// width; the autotuner picks it per batch).  The strided staging layout is
+// conflict-free at every width; the padded exchange layout (one spare word
+// per 32) is conflict-free at 32 and leaves some two-way conflicts at 16.
 #pragma once
 
 #include "device.cuh"
