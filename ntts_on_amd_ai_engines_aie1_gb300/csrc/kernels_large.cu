@@ -56,21 +56,29 @@ __global__ void __launch_bounds__(P << (L2 - LARGE_EL)) k_rows(const __grid_cons
     const int hi = (int)(row & ((1LL << L1) - 1));               // row index inside its polynomial
     int* sp = rsmem + lp * xwords(L2);
     int v[E];
+    // rows are contiguous: every thread moves E consecutive coefficients with
+    // 16-byte accesses, and the exchange buffer turns them into (and back
+    // from) the transform's first (last) window
     if (active) {
-        const int* src = static_cast<const int*>(a.in) + row * N;
+        const int4* src = reinterpret_cast<const int4*>(static_cast<const int*>(a.in) + row * N) + g * (E / 4);
 #pragma unroll
-        for (int k = 0; k < E; ++k) v[k] = __ldg(src + posmap<LO0, EL>(g, k));
+        for (int j = 0; j < E / 4; ++j) {
+            const int4 w = __ldg(src + j);
+            v[4 * j] = w.x; v[4 * j + 1] = w.y; v[4 * j + 2] = w.z; v[4 * j + 3] = w.w;
+        }
     } else {
 #pragma unroll
         for (int k = 0; k < E; ++k) v[k] = 0;
     }
+    if constexpr (LO0 != 0) exchange_windows<L2, EL, 0, LO0>(v, sp, g);
     const KC kc = make_kc(a);
     run_steps_x<FAM, L2, EL, 0, true>(v, sp, g, kc, hi, 0, std::make_integer_sequence<int, NS>{});
     epilogue_all<false>(v, a);
+    if constexpr (LOZ != 0) exchange_windows<L2, EL, LOZ, 0>(v, sp, g);
     if (active) {
-        int* dst = static_cast<int*>(a.out) + row * N;
+        int4* dst = reinterpret_cast<int4*>(static_cast<int*>(a.out) + row * N) + g * (E / 4);
 #pragma unroll
-        for (int k = 0; k < E; ++k) dst[posmap<LOZ, EL>(g, k)] = v[k];
+        for (int j = 0; j < E / 4; ++j) dst[j] = make_int4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
     }
 }
 
