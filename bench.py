@@ -488,7 +488,7 @@ def run_serving(gb, seconds):
     above 4096 and no int16-storable prime below the lazy-reduction bound has
     one of order 8192, so int16 requests draw U again from {8..12}.  Host
     buffers are pinned.  A saturating burst measures the capacity; open-loop
-    Poisson arrivals at 50% and 90% of it give p50/p99 latency (submit to
+    Poisson arrivals at 50%, 90% and 100% of it give p50/p99 latency (submit to
     result in host memory).  A sample of requests is checked against the same
     transform launched alone."""
     import torch
@@ -562,7 +562,7 @@ def run_serving(gb, seconds):
            "saturation": {"requests_per_s": cap, "NTT_per_s": cap, "algorithmic_GBps": nbytes / el / 1e9,
                           "requests": nsat, "microbatches": st["microbatches"], "launches": st["launches"],
                           "p50_us": st["p50_us"], "p99_us": st["p99_us"]}}
-    for frac in (0.5, 0.9):
+    for frac in (0.5, 0.9, 1.0):
         rate = frac * cap
         nreq = int(min(200000, max(1000, rate * seconds)))
         arrivals = np.cumsum(rng.exponential(1e6 / rate, nreq)).tolist()

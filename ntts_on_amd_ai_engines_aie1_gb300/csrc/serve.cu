@@ -597,14 +597,15 @@ int gbntt_server_create(gbntt_server** out, const gbntt_plan* const* plans, uint
     return GBNTT_OK;
 }
 
-int gbntt_server_submit(gbntt_server* s, uint32_t plan, const void* h_in, void* h_out, uint64_t count,
-                        uint64_t* ticket) {
+namespace {
+
+// queues one request whose host buffers' device addresses are already known
+int enqueue(gbntt_server* s, uint32_t plan, const void* h_in, void* h_out, uint64_t count, uint64_t* ticket,
+            const void* m_in, void* m_out) {
     if (!s || !ticket) return sfail(GBNTT_ERR_ARG, "null argument");
     if (plan >= s->plans.size()) return sfail(GBNTT_ERR_ARG, "plan index out of range");
     if (!h_in || !h_out || !count) return sfail(GBNTT_ERR_ARG, "request without data");
     const size_t bytes = (size_t)count * (size_t)s->plan_bytes[plan];
-    const void* m_in = gbntt_internal_mapped(h_in);
-    void* m_out = const_cast<void*>(gbntt_internal_mapped(h_out));
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->worker_error) return sfail(s->worker_error, s->worker_msg);
     const uint64_t t = s->next_ticket++;
@@ -619,6 +620,15 @@ int gbntt_server_submit(gbntt_server* s, uint32_t plan, const void* h_in, void* 
     s->pending.push_back(Request{t, plan, h_in, h_out, count, bytes, Clock::now(), m_in, m_out});
     s->cv_work.notify_one();
     return GBNTT_OK;
+}
+
+}  // namespace
+
+int gbntt_server_submit(gbntt_server* s, uint32_t plan, const void* h_in, void* h_out, uint64_t count,
+                        uint64_t* ticket) {
+    if (!h_in || !h_out) return sfail(GBNTT_ERR_ARG, "request without data");
+    return enqueue(s, plan, h_in, h_out, count, ticket, gbntt_internal_mapped(h_in),
+                   const_cast<void*>(gbntt_internal_mapped(h_out)));
 }
 
 int gbntt_server_wait(gbntt_server* s, uint64_t ticket, uint32_t timeout_ms) {
@@ -710,12 +720,28 @@ int gbntt_server_submit_schedule(gbntt_server* s, uint64_t nreq, const uint32_t*
                                  const double* arrival_us, uint64_t* tickets) {
     if (!s || (nreq && (!plan || !h_in || !h_out || !count || !arrival_us || !tickets)))
         return sfail(GBNTT_ERR_ARG, "null argument");
+    // The caller keeps every buffer of the schedule alive for the whole call,
+    // so each distinct buffer's device address is looked up once.
+    std::unordered_map<const void*, const void*> mapped;
+    auto lookup = [&](const void* h) {
+        auto it = mapped.find(h);
+        if (it != mapped.end()) return it->second;
+        const void* m = gbntt_internal_mapped(h);
+        mapped.emplace(h, m);
+        return m;
+    };
+    for (uint64_t i = 0; i < nreq; ++i) {   // resolve before the clock starts
+        if (h_in[i]) lookup(h_in[i]);
+        if (h_out[i]) lookup(h_out[i]);
+    }
     const auto t0 = Clock::now();
     for (uint64_t i = 0; i < nreq; ++i) {
         const auto due = t0 + std::chrono::nanoseconds((long long)(arrival_us[i] * 1000.0));
         while (Clock::now() < due) {
         }
-        const int rc = gbntt_server_submit(s, plan[i], h_in[i], h_out[i], count[i], &tickets[i]);
+        if (!h_in[i] || !h_out[i]) return sfail(GBNTT_ERR_ARG, "request without data");
+        const int rc = enqueue(s, plan[i], h_in[i], h_out[i], count[i], &tickets[i], lookup(h_in[i]),
+                               const_cast<void*>(lookup(h_out[i])));
         if (rc != GBNTT_OK) return rc;
     }
     return GBNTT_OK;
