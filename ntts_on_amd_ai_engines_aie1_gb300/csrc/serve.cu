@@ -261,6 +261,7 @@ void finish_slot(gbntt_server* s, Slot& sl) {
 // Issue one micro-batch on slot sl: gather (kernel for mapped requests, copy
 // engine for the others), one in-place launch per plan group, scatter, event.
 int issue(gbntt_server* s, Slot& sl) {
+    uint64_t nl = 0;   // launches of this micro-batch (published under the lock at the end)
     int nin = 0;
     unsigned long long cin = 0;
     for (auto& g : sl.groups) {               // gather descriptors
@@ -297,7 +298,7 @@ int issue(gbntt_server* s, Slot& sl) {
     if (nin) {
         k_copy_desc<<<(unsigned)cin, COPY_THREADS, 0, sl.stream>>>(sl.d_desc, nin);
         gbntt_internal_count_launch();
-        ++s->launches;
+        ++nl;
     }
     for (auto& g : sl.groups) {
         char* base = s->d_arena + g.off;
@@ -354,14 +355,14 @@ int issue(gbntt_server* s, Slot& sl) {
             e = cudaLaunchKernel(pc.cfg->fn, dim3(grid), dim3(BATCH_CTA), args, pc.smem, sl.stream);
             if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve launch: ") + cudaGetErrorString(e));
             gbntt_internal_count_launch();
-            ++s->launches;
+            ++nl;
         }
         for (const Group* g : order) {
             if (s->pinfo[g->plan].part >= 0) continue;
             const int rc = gbntt_execute(s->plans[g->plan], s->d_arena + g->off, s->d_arena + g->off, g->count,
                                          sl.stream);
             if (rc != GBNTT_OK) return rc;
-            ++s->launches;
+            ++nl;
         }
         // the persistent launches' error words come back with the results
         e = cudaMemcpyAsync(sl.h_err, sl.d_ctr, 2 * CTR_WORDS * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
@@ -371,7 +372,7 @@ int issue(gbntt_server* s, Slot& sl) {
     if (nout) {
         k_copy_desc<<<(unsigned)cout, COPY_THREADS, 0, sl.stream>>>(sl.d_desc + nin, nout);
         gbntt_internal_count_launch();
-        ++s->launches;
+        ++nl;
     }
     for (auto& g : sl.groups) {
         char* base = s->d_arena + g.off;
@@ -389,6 +390,8 @@ int issue(gbntt_server* s, Slot& sl) {
     e = cudaEventRecord(sl.done, sl.stream);
     if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve event: ") + cudaGetErrorString(e));
     sl.busy = true;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->launches += nl;
     ++s->microbatches;
     return GBNTT_OK;
 }
