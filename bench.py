@@ -544,12 +544,12 @@ def run_serving(gb, seconds):
     def run(nreq, arrivals):
         srv.stats(reset=True)
         idx, ins, outl, nbytes = draw(nreq)
-        t0 = time.perf_counter()
         srv.submit_schedule(idx, ins, outl, [1] * nreq, arrivals)
         srv.drain()
-        el = time.perf_counter() - t0
         st = srv.stats()
         assert st["completed"] == nreq and st["refused"] == 0
+        # the server's own clock: first arrival to last completion (single-polynomial requests)
+        el = nreq / st["polys_per_s"]
         return st, el, nbytes
 
     run(5000, [0.0] * 5000)                                         # warm-up

@@ -212,14 +212,21 @@ struct gbntt_server {
     uint32_t max_group_requests = 0;
     int device = 0;
 
-    std::mutex mu;
-    std::condition_variable cv_work, cv_done;
-    std::deque<Request> pending;
-    std::unordered_map<uint64_t, int> status;   // ticket -> status (absent: in flight)
-    uint64_t next_ticket = 1;
-    bool stop = false;
+    // submissions: a short-held inbox the worker swaps out, so submitting never
+    // waits for the worker's micro-batch formation
+    std::mutex inbox_mu;
+    std::condition_variable cv_work;           // with inbox_mu: new requests or stop
+    std::vector<Request> inbox;
+    std::deque<Request> pending;               // the worker's own queue (arrival order)
+    std::atomic<uint64_t> next_ticket{1};
+    std::atomic<long long> outstanding{0};     // admitted and not yet completed
+    std::atomic<bool> stop{false};
+    std::atomic<int> worker_error{GBNTT_OK};
     std::thread worker;
-    int worker_error = GBNTT_OK;
+
+    std::mutex mu;                             // status, statistics, worker_msg
+    std::condition_variable cv_done;           // with mu: completions
+    std::unordered_map<uint64_t, int> status;  // ticket -> status (absent: in flight)
     std::string worker_msg;
 
     // statistics (guarded by mu)
@@ -233,29 +240,36 @@ namespace {
 
 int sfail(int code, const std::string& m) { return gbntt_internal_fail(code, m); }
 
+// the worker thread's error: stops the loop and fails every later wait
+void set_worker_error(gbntt_server* s, int code, const std::string& msg) {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->worker_msg = msg;
+    s->worker_error = code;
+    s->stop = true;
+    s->cv_done.notify_all();
+}
+
 void finish_slot(gbntt_server* s, Slot& sl) {
     const auto now = Clock::now();
+    if (sl.h_err[CTR_ERROR] || sl.h_err[CTR_WORDS + CTR_ERROR])   // a tile load ran out of its wait limit
+        set_worker_error(s, GBNTT_ERR_TIMEOUT, "serve: a tile load did not arrive within the wait limit");
+    long long done = 0;
     std::lock_guard<std::mutex> lk(s->mu);
-    if (sl.h_err[CTR_ERROR] || sl.h_err[CTR_WORDS + CTR_ERROR]) {
-        // a tile load did not arrive within the persistent kernel's wait limit
-        s->worker_error = GBNTT_ERR_TIMEOUT;
-        s->worker_msg = "serve: a tile load did not arrive within the wait limit";
-        s->stop = true;
-    }
     for (auto& g : sl.groups) {
-        s->arena.release(g.off, g.bytes);
+        s->arena.release(g.off, g.bytes);   // the arena is the worker's; released under mu for the stats
         for (auto& r : g.reqs) {
             s->status[r.ticket] = GBNTT_OK;
             s->lat_us.push_back(std::chrono::duration<double, std::micro>(now - r.t_submit).count());
             s->polys += r.count;
             ++s->completed;
+            ++done;
         }
     }
     s->t_last = now;
     sl.groups.clear();
     sl.busy = false;
+    s->outstanding -= done;
     s->cv_done.notify_all();
-    s->cv_work.notify_all();
 }
 
 // Issue one micro-batch on slot sl: gather (kernel for mapped requests, copy
@@ -406,73 +420,75 @@ void worker_main(gbntt_server* s) {
             const cudaError_t q = cudaEventQuery(sl.done);
             if (q == cudaSuccess) finish_slot(s, sl);
             else if (q == cudaErrorNotReady) any_busy = true;
-            else {
-                std::lock_guard<std::mutex> lk(s->mu);
-                s->worker_error = GBNTT_ERR_CUDA;
-                s->worker_msg = std::string("serve: ") + cudaGetErrorString(q);
-                s->stop = true;
+            else set_worker_error(s, GBNTT_ERR_CUDA, std::string("serve: ") + cudaGetErrorString(q));
+        }
+        // 2. new requests
+        {
+            std::lock_guard<std::mutex> lk(s->inbox_mu);
+            if (!s->inbox.empty()) {
+                if (s->pending.empty()) {   // the first request since the statistics were reset
+                    std::lock_guard<std::mutex> lk2(s->mu);
+                    if (s->completed == 0 && s->microbatches == 0) s->t_first = Clock::now();
+                }
+                for (auto& r : s->inbox) s->pending.push_back(r);
+                s->inbox.clear();
             }
         }
-        // 2. admission into a free slot
+        if (s->stop && (s->pending.empty() || s->worker_error) && !any_busy) {
+            std::lock_guard<std::mutex> lk(s->inbox_mu);
+            if (s->inbox.empty() || s->worker_error) break;
+            continue;
+        }
+        // 3. admission into a free slot: waiting requests in arrival order while the arena has room
         Slot* free_slot = nullptr;
         for (auto& sl : s->slots)
             if (!sl.busy) { free_slot = &sl; break; }
         std::vector<Group> groups;
-        {
-            std::unique_lock<std::mutex> lk(s->mu);
-            if (s->stop && (s->pending.empty() || s->worker_error)) {
-                if (!any_busy) break;
-            }
-            if (free_slot && !s->pending.empty()) {
-                // take waiting requests in arrival order while the arena has room
-                std::map<uint32_t, size_t> gi;
-                uint32_t taken = 0;
-                size_t mb_bytes = 0;
-                const size_t budget = s->arena.capacity() / s->slots.size();   // one slot's share
-                while (!s->pending.empty() && taken < s->max_group_requests) {
-                    Request& r = s->pending.front();
-                    if (taken && mb_bytes + r.bytes > budget) break;
-                    mb_bytes += r.bytes;
-                    auto it = gi.find(r.plan);
-                    Group* g;
-                    if (it == gi.end()) {
-                        gi[r.plan] = groups.size();
-                        groups.push_back(Group());
-                        g = &groups.back();
-                        g->plan = r.plan;
-                    } else {
-                        g = &groups[it->second];
-                    }
-                    g->reqs.push_back(r);
-                    g->count += r.count;
-                    g->bytes += r.bytes;
-                    s->pending.pop_front();
-                    ++taken;
+        if (free_slot && !s->pending.empty() && !s->worker_error) {
+            std::map<uint32_t, size_t> gi;
+            uint32_t taken = 0;
+            size_t mb_bytes = 0;
+            const size_t budget = s->arena.capacity() / s->slots.size();   // one slot's share
+            while (!s->pending.empty() && taken < s->max_group_requests) {
+                Request& r = s->pending.front();
+                if (taken && mb_bytes + r.bytes > budget) break;
+                mb_bytes += r.bytes;
+                auto it = gi.find(r.plan);
+                Group* g;
+                if (it == gi.end()) {
+                    gi[r.plan] = groups.size();
+                    groups.push_back(Group());
+                    g = &groups.back();
+                    g->plan = r.plan;
+                } else {
+                    g = &groups[it->second];
                 }
-                // reserve one arena block per group; what does not fit goes back to the queue front
-                for (size_t i = groups.size(); i-- > 0;) {
-                    Group& g = groups[i];
-                    g.off = s->arena.alloc(g.bytes);
-                    if (g.off == SIZE_MAX) {
-                        for (auto r = g.reqs.rbegin(); r != g.reqs.rend(); ++r) s->pending.push_front(*r);
-                        groups.erase(groups.begin() + (long)i);
-                    }
-                }
-                s->peak_used = std::max(s->peak_used, s->arena.used());
-            } else if (!any_busy && s->pending.empty() && !s->stop) {
-                s->cv_work.wait_for(lk, std::chrono::milliseconds(2));
-                continue;
+                g->reqs.push_back(r);
+                g->count += r.count;
+                g->bytes += r.bytes;
+                s->pending.pop_front();
+                ++taken;
             }
+            // one arena block per group; what does not fit goes back to the front of the queue
+            std::lock_guard<std::mutex> lk(s->mu);
+            for (size_t i = groups.size(); i-- > 0;) {
+                Group& g = groups[i];
+                g.off = s->arena.alloc(g.bytes);
+                if (g.off == SIZE_MAX) {
+                    for (auto r = g.reqs.rbegin(); r != g.reqs.rend(); ++r) s->pending.push_front(*r);
+                    groups.erase(groups.begin() + (long)i);
+                }
+            }
+            s->peak_used = std::max(s->peak_used, s->arena.used());
+        } else if (!any_busy && s->pending.empty()) {
+            std::unique_lock<std::mutex> lk(s->inbox_mu);
+            s->cv_work.wait_for(lk, std::chrono::milliseconds(2), [&] { return !s->inbox.empty() || s->stop; });
+            continue;
         }
         if (!groups.empty()) {
             free_slot->groups = std::move(groups);
             const int rc = issue(s, *free_slot);
-            if (rc != GBNTT_OK) {
-                std::lock_guard<std::mutex> lk(s->mu);
-                s->worker_error = rc;
-                s->worker_msg = gbntt_last_error();
-                s->stop = true;
-            }
+            if (rc != GBNTT_OK) set_worker_error(s, rc, gbntt_last_error());
         } else if (any_busy) {
             std::this_thread::yield();
         }
@@ -609,18 +625,24 @@ int enqueue(gbntt_server* s, uint32_t plan, const void* h_in, void* h_out, uint6
     if (plan >= s->plans.size()) return sfail(GBNTT_ERR_ARG, "plan index out of range");
     if (!h_in || !h_out || !count) return sfail(GBNTT_ERR_ARG, "request without data");
     const size_t bytes = (size_t)count * (size_t)s->plan_bytes[plan];
-    std::lock_guard<std::mutex> lk(s->mu);
-    if (s->worker_error) return sfail(s->worker_error, s->worker_msg);
+    if (s->worker_error) {
+        std::lock_guard<std::mutex> lk(s->mu);
+        return sfail(s->worker_error, s->worker_msg);
+    }
     const uint64_t t = s->next_ticket++;
     *ticket = t;
     if ((bytes + Arena::ALIGN - 1) / Arena::ALIGN * Arena::ALIGN > s->arena.capacity()) {
+        std::lock_guard<std::mutex> lk(s->mu);
         s->status[t] = GBNTT_ERR_ADMISSION;   // can never fit: refused, not queued
         ++s->refused;
         s->cv_done.notify_all();
         return GBNTT_OK;
     }
-    if (s->completed == 0 && s->pending.empty() && s->microbatches == 0) s->t_first = Clock::now();
-    s->pending.push_back(Request{t, plan, h_in, h_out, count, bytes, Clock::now(), m_in, m_out});
+    ++s->outstanding;
+    {
+        std::lock_guard<std::mutex> lk(s->inbox_mu);
+        s->inbox.push_back(Request{t, plan, h_in, h_out, count, bytes, Clock::now(), m_in, m_out});
+    }
     s->cv_work.notify_one();
     return GBNTT_OK;
 }
@@ -658,11 +680,9 @@ int gbntt_server_drain(gbntt_server* s, uint32_t timeout_ms) {
     std::unique_lock<std::mutex> lk(s->mu);
     const auto deadline = Clock::now() + std::chrono::milliseconds(timeout_ms);
     for (;;) {
-        bool busy = !s->pending.empty();
-        for (auto& sl : s->slots) busy = busy || sl.busy;
-        if (!busy) return GBNTT_OK;
+        if (s->outstanding.load() == 0) return GBNTT_OK;
         if (s->worker_error) return sfail(s->worker_error, s->worker_msg);
-        if (s->cv_done.wait_until(lk, deadline) == std::cv_status::timeout)
+        if (s->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && s->outstanding.load() != 0)
             return sfail(GBNTT_ERR_TIMEOUT, "server did not drain within the timeout");
     }
 }
@@ -695,10 +715,10 @@ int gbntt_server_get_stats(gbntt_server* s, gbntt_server_stats* st, int reset) {
 int gbntt_server_destroy(gbntt_server* s) {
     if (!s) return GBNTT_OK;
     {
-        std::lock_guard<std::mutex> lk(s->mu);
+        std::lock_guard<std::mutex> lk(s->inbox_mu);
         s->stop = true;
-        s->cv_work.notify_all();
     }
+    s->cv_work.notify_all();
     if (s->worker.joinable()) s->worker.join();
     for (auto& sl : s->slots) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
