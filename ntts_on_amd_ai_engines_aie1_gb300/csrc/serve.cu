@@ -486,8 +486,33 @@ void worker_main(gbntt_server* s) {
             continue;
         }
         if (!groups.empty()) {
+            // Groups that run their plan's own launches (int32 n >= 2^16 two-pass,
+            // radix-4 inverse, ...) take longer than the persistent launch: with a
+            // second free slot they form their own micro-batch, so the other
+            // requests complete without waiting for them.
+            std::vector<Group> slow;
+            for (auto it = groups.begin(); it != groups.end();) {
+                if (s->pinfo[it->plan].part < 0) {
+                    slow.push_back(std::move(*it));
+                    it = groups.erase(it);
+                } else {
+                    ++it;
+                }
+            }
+            Slot* second = nullptr;
+            if (!slow.empty() && !groups.empty())
+                for (auto& sl : s->slots)
+                    if (!sl.busy && &sl != free_slot) { second = &sl; break; }
+            if (!second) {
+                for (auto& g : slow) groups.push_back(std::move(g));
+                slow.clear();
+            }
             free_slot->groups = std::move(groups);
-            const int rc = issue(s, *free_slot);
+            int rc = issue(s, *free_slot);
+            if (rc == GBNTT_OK && second) {
+                second->groups = std::move(slow);
+                rc = issue(s, *second);
+            }
             if (rc != GBNTT_OK) set_worker_error(s, rc, gbntt_last_error());
         } else if (any_busy) {
             std::this_thread::yield();
