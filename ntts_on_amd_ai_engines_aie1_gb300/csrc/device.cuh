@@ -224,36 +224,122 @@ __host__ __device__ constexpr int r8_stage_offset(int L, int s) {
 // padded shared-memory index of a position (one spare word every 32)
 __device__ __forceinline__ int spad(int pos) { return pos + (pos >> 5); }
 
-// shared-memory words per polynomial of the exchange buffer (16-byte multiple)
-__host__ __device__ constexpr int xwords(int L) { return (((1 << L) + (1 << L) / 32) + 3) & ~3; }
-
-// Vectorised exchange layout.  When the windows before and after an exchange
-// share position bits [OLO, OLO + VB), the 2^VB values that differ only in
-// those bits stay in one thread on both sides and move as one 8- or 16-byte
-// access.  The word address keeps those bits lowest; the chunk index (the
-// remaining bits) is XOR-folded so that the chunks of a quarter warp spread
-// over all banks.
-template <int OLO, int VB>
-__device__ __forceinline__ int vaddr(int pos) {
-    const int low = (pos >> OLO) & ((1 << VB) - 1);
-    int c = ((pos >> (OLO + VB)) << OLO) | (pos & ((1 << OLO) - 1));
-    if constexpr (VB == 2) c ^= ((c >> 3) ^ (c >> 6) ^ (c >> 9) ^ (c >> 12)) & 7;
-    else c ^= ((c >> 4) ^ (c >> 8) ^ (c >> 12)) & 15;
-    return (c << VB) | low;
-}
-
-template <int G>
-__device__ __forceinline__ void group_sync();
-
-// Moves the thread's registers from the window starting at bit LOA to the
-// window starting at LOB through the shared buffer sp.
-template <int L, int EL, int LOA, int LOB>
-__device__ __forceinline__ void exchange_windows(int (&v)[1 << EL], int* sp, int g);
+// shared-memory words per polynomial of the exchange buffer (16-byte
+// multiple): room for the padded exchange layouts below (at most one spare
+// word per 16 positions)
+__host__ __device__ constexpr int xwords(int L) { return (((1 << L) + (1 << L) / 16) + 3) & ~3; }
 
 // position of register k of thread g when the window starts at bit LO
-template <int LO, int EL>
-__device__ __forceinline__ int posmap(int g, int k) {
+__host__ __device__ constexpr int posmap_c(int LO, int EL, int g, int k) {
     return ((g >> LO) << (LO + EL)) | (k << LO) | (g & ((1 << LO) - 1));
+}
+template <int LO, int EL>
+__device__ __forceinline__ int posmap(int g, int k) { return posmap_c(LO, EL, g, k); }
+
+// ---------------------------------------------------------------------------
+// Exchange layouts.  An exchange writes every register of the window starting
+// at bit LOA and reads back the window starting at LOB.  Both access patterns
+// are fixed at compile time, so each exchange gets its own layout, chosen so
+// that the 32 lanes of a warp hit distinct banks on both sides (lanes past a
+// short polynomial belong to the next one, xwords(L) words further).
+//
+// Scalar exchanges (no position bit shared by the two windows): word =
+// pos + (pos >> S) * T, one to two spare words every 32.  The padding is a sum
+// over disjoint bit fields, so the address of register k is the thread's base
+// plus a compile-time constant.
+//
+// Vectorised exchanges: when the windows share position bits [OLO, OLO + VB),
+// the 2^VB values that differ only in those bits stay in one thread on both
+// sides and move as one 8- or 16-byte access.  The word address keeps those
+// bits lowest; the remaining bits form the chunk index c, whose bank-group
+// bits are XOR-folded with c >> F (F = 0: no fold).  The fold is linear, so the
+// register-dependent part is again a compile-time constant.
+// ---------------------------------------------------------------------------
+
+__host__ __device__ constexpr int xpad(int p, int s, int t) { return p + (p >> s) * t; }
+
+// bank-conflict degree summed over both sides (2 = conflict free)
+__host__ __device__ constexpr int scalar_degree(int L, int EL, int LOA, int LOB, int s, int t) {
+    const int G = 1 << (L - EL);
+    int total = 0;
+    for (int side = 0; side < 2; ++side) {
+        int cnt[32] = {};
+        int worst = 0;
+        for (int lane = 0; lane < 32; ++lane) {
+            const int w = (lane / G) * xwords(L) + xpad(posmap_c(side ? LOB : LOA, EL, lane % G, 0), s, t);
+            const int c = ++cnt[w & 31];
+            worst = c > worst ? c : worst;
+        }
+        total += worst;
+    }
+    return total;
+}
+
+struct XPad { int s, t; };
+
+// the padding of a scalar exchange: fewest conflicts, then the first candidate
+__host__ __device__ constexpr XPad scalar_layout(int L, int EL, int LOA, int LOB) {
+    XPad best{5, 1};
+    int bd = scalar_degree(L, EL, LOA, LOB, 5, 1);
+    for (int s = 4; s <= L && bd > 2; ++s)
+        for (int t = 1; t <= 16 && bd > 2; t *= 2) {
+            if (t * 32 > (2 << s) || xpad((1 << L) - 1, s, t) >= xwords(L)) continue;
+            const int d = scalar_degree(L, EL, LOA, LOB, s, t);
+            if (d < bd) { bd = d; best = XPad{s, t}; }
+        }
+    return best;
+}
+
+__host__ __device__ constexpr int vchunk(int pos, int OLO, int VB) {
+    return ((pos >> (OLO + VB)) << OLO) | (pos & ((1 << OLO) - 1));
+}
+// fold of the chunk index: bank-group bits (5 - VB of them) XOR c >> F
+__host__ __device__ constexpr int vfold(int c, int VB, int F) {
+    return F ? c ^ ((c >> F) & ((1 << (5 - VB)) - 1)) : c;
+}
+__host__ __device__ constexpr int vword(int pos, int OLO, int VB, int F) {
+    return (vfold(vchunk(pos, OLO, VB), VB, F) << VB) | ((pos >> OLO) & ((1 << VB) - 1));
+}
+
+// shared-memory wavefronts of one warp over both sides of a vectorised
+// exchange (a 16-byte access is served per quarter warp, an 8-byte access per
+// half warp)
+__host__ __device__ constexpr int vector_wavefronts(int L, int EL, int LOA, int LOB, int VB, int F) {
+    const int G = 1 << (L - EL), E = 1 << EL, V = 1 << VB;
+    const int OLO = LOA > LOB ? LOA : LOB;
+    const int per = 8 * (4 / V);            // lanes per phase
+    int total = 0;
+    for (int side = 0; side < 2; ++side) {
+        const int LO = side ? LOB : LOA, KX = OLO - LO;
+        for (int r = 0; r < (E >> VB); ++r) {
+            const int k = ((r >> KX) << (KX + VB)) | (r & ((1 << KX) - 1));
+            for (int ph = 0; ph < 32 / per; ++ph) {
+                int cnt[32] = {};
+                int worst = 0;
+                for (int lane = ph * per; lane < (ph + 1) * per; ++lane) {
+                    const int w = (lane / G) * xwords(L) + vword(posmap_c(LO, EL, lane % G, k), OLO, VB, F);
+                    for (int j = 0; j < V; ++j) {
+                        const int c = ++cnt[(w + j) & 31];
+                        worst = c > worst ? c : worst;
+                    }
+                }
+                total += worst;
+            }
+        }
+    }
+    return total;
+}
+
+// the fold of a vectorised exchange: fewest wavefronts, no fold on a tie
+__host__ __device__ constexpr int vector_layout(int L, int EL, int LOA, int LOB, int VB) {
+    int best = 0;
+    int bw = vector_wavefronts(L, EL, LOA, LOB, VB, 0);
+    const int ideal = 2 * (1 << EL);        // E / V accesses of V wavefronts per side
+    for (int f = 1; f < L - VB && bw > ideal; ++f) {
+        const int w = vector_wavefronts(L, EL, LOA, LOB, VB, f);
+        if (w < bw) { bw = w; best = f; }
+    }
+    return best;
 }
 
 template <int G>
@@ -262,6 +348,8 @@ __device__ __forceinline__ void group_sync() {
     else __syncwarp();
 }
 
+// Moves the thread's registers from the window starting at bit LOA to the
+// window starting at LOB through the shared buffer sp.
 template <int L, int EL, int LOA, int LOB>
 __device__ __forceinline__ void exchange_windows(int (&v)[1 << EL], int* sp, int g) {
     constexpr int E = 1 << EL, G = 1 << (L - EL);
@@ -271,18 +359,26 @@ __device__ __forceinline__ void exchange_windows(int (&v)[1 << EL], int* sp, int
     constexpr int VB = W >= 2 ? 2 : W;
     group_sync<G>();
     if constexpr (VB == 0) {
+        constexpr XPad X = scalar_layout(L, EL, LOA, LOB);
+        int* const pa = sp + xpad(posmap<LOA, EL>(g, 0), X.s, X.t);
 #pragma unroll
-        for (int k = 0; k < E; ++k) sp[spad(posmap<LOA, EL>(g, k))] = v[k];
+        for (int k = 0; k < E; ++k) pa[xpad(k << LOA, X.s, X.t)] = v[k];
         group_sync<G>();
+        const int* const pb = sp + xpad(posmap<LOB, EL>(g, 0), X.s, X.t);
 #pragma unroll
-        for (int k = 0; k < E; ++k) v[k] = sp[spad(posmap<LOB, EL>(g, k))];
+        for (int k = 0; k < E; ++k) v[k] = pb[xpad(k << LOB, X.s, X.t)];
     } else {
-        constexpr int KA = OLO - LOA, KB = OLO - LOB;   // register bit of the shared bits
-        constexpr int V = 1 << VB;
+        constexpr int F = vector_layout(L, EL, LOA, LOB, VB);
+        constexpr int V = 1 << VB, MB = (1 << (5 - VB)) - 1;   // bank-group bits of the chunk
+        constexpr int KA = OLO - LOA, KB = OLO - LOB;           // register bit of the shared bits
+        // chunk word of the thread's part of the position; the register part
+        // is XORed into the bank-group bits and added above them
+        const int xa = vfold(vchunk(posmap<LOA, EL>(g, 0), OLO, VB), VB, F) << VB;
 #pragma unroll
         for (int r = 0; r < (E >> VB); ++r) {
             const int k = ((r >> KA) << (KA + VB)) | (r & ((1 << KA) - 1));
-            const int a = vaddr<OLO, VB>(posmap<LOA, EL>(g, k));
+            const int kc = vfold(vchunk(k << LOA, OLO, VB), VB, F);
+            const int a = (xa ^ ((kc & MB) << VB)) + ((kc & ~MB) << VB);
             if constexpr (V == 4)
                 *reinterpret_cast<int4*>(sp + a) =
                     make_int4(v[k], v[k | (1 << KA)], v[k | (2 << KA)], v[k | (3 << KA)]);
@@ -290,10 +386,12 @@ __device__ __forceinline__ void exchange_windows(int (&v)[1 << EL], int* sp, int
                 *reinterpret_cast<int2*>(sp + a) = make_int2(v[k], v[k | (1 << KA)]);
         }
         group_sync<G>();
+        const int xb = vfold(vchunk(posmap<LOB, EL>(g, 0), OLO, VB), VB, F) << VB;
 #pragma unroll
         for (int r = 0; r < (E >> VB); ++r) {
             const int k = ((r >> KB) << (KB + VB)) | (r & ((1 << KB) - 1));
-            const int a = vaddr<OLO, VB>(posmap<LOB, EL>(g, k));
+            const int kc = vfold(vchunk(k << LOB, OLO, VB), VB, F);
+            const int a = (xb ^ ((kc & MB) << VB)) + ((kc & ~MB) << VB);
             if constexpr (V == 4) {
                 const int4 w = *reinterpret_cast<const int4*>(sp + a);
                 v[k] = w.x; v[k | (1 << KB)] = w.y; v[k | (2 << KB)] = w.z; v[k | (3 << KB)] = w.w;
