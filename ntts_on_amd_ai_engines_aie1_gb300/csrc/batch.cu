@@ -21,6 +21,7 @@ struct gbntt_batch {
         BatchConfig cfg{};
         std::vector<SegDev> segs;
         SegDev* d_segs = nullptr;
+        std::vector<SegDev> live;       // zero-copy layout: the descriptors d_segs holds now
         long long total_tiles = 0;
         int stage_bytes = 0, smem = 0, grid = 0;
         float ms = -1.f;                // autotuner timing
@@ -145,6 +146,8 @@ struct ZcPlanState {
     int stage = 0, smem = 0, grid_cap = 0;
     SegDev* d_seg = nullptr;
     unsigned long long* d_ctr = nullptr;
+    SegDev live{};              // the descriptor d_seg holds (valid when has_live)
+    bool has_live = false;
 };
 
 }  // namespace
@@ -198,8 +201,15 @@ int gbntt_internal_zc_plan(void** state, const gbntt_plan* p, const void* m_in, 
     sd.variant = variant_id(fam, L);
     sd.polys_per_tile = st.cfg.cta >> (L - batch_el(L, st.cfg.elmax));
     sd.tiles = ((long long)count + sd.polys_per_tile - 1) / sd.polys_per_tile;
-    cudaError_t e = cudaMemcpyAsync(st.d_seg, &sd, sizeof(SegDev), cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("descriptor: ") + cudaGetErrorString(e));
+    // repeated calls on the same buffers reuse the descriptor already on the device
+    cudaError_t e = cudaSuccess;
+    if (!st.has_live || std::memcmp(&st.live, &sd, sizeof(SegDev)) != 0) {
+        st.has_live = false;
+        e = cudaMemcpyAsync(st.d_seg, &sd, sizeof(SegDev), cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("descriptor: ") + cudaGetErrorString(e));
+        st.live = sd;
+        st.has_live = true;
+    }
     BatchDev bd;
     bd.segs = st.d_seg;
     bd.nsegs = 1;
@@ -209,7 +219,10 @@ int gbntt_internal_zc_plan(void** state, const gbntt_plan* p, const void* m_in, 
     void* args[] = {&bd, &sb};
     const unsigned grid = (unsigned)std::min<long long>(st.grid_cap, sd.tiles);
     e = cudaLaunchKernel(st.cfg.zfn, dim3(grid), dim3(st.cfg.cta), args, st.smem, s);
-    if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("zero-copy launch: ") + cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+        st.has_live = false;
+        return batch_fail(GBNTT_ERR_CUDA, std::string("zero-copy launch: ") + cudaGetErrorString(e));
+    }
     gbntt_internal_count_launch();
     return GBNTT_OK;
 }
@@ -423,14 +436,16 @@ int gbntt_batch_execute_host(gbntt_batch* b, const void* const* h_in, void* cons
     // instead of running as two copy phases.  Segments outside the persistent
     // kernel still go through their device buffers.
     bool zero_copy = true;
+    std::vector<const void*> mapped_in(b->user.size()), mapped_out(b->user.size());
     for (size_t k = 0; k < b->user.size() && zero_copy; ++k) {
         if (b->part_of[k] < 0 || !bytes_of(k)) continue;
-        const void* mi = gbntt_internal_mapped(h_in[k]);
-        const void* mo = gbntt_internal_mapped(h_out[k]);
+        const void* mi = mapped_in[k] = gbntt_internal_mapped(h_in[k]);
+        const void* mo = mapped_out[k] = gbntt_internal_mapped(h_out[k]);
         zero_copy = b->parts[b->part_of[k]].zlay.cfg.zfn && mi && mo &&
                     !((reinterpret_cast<uintptr_t>(mi) | reinterpret_cast<uintptr_t>(mo)) & 15);
     }
     if (zero_copy) {
+        std::vector<SegDev> uploaded[2];   // committed as the live descriptors once the call completed
         for (int i = 0; i < b->nparts; ++i) {
             auto& part = b->parts[i];
             auto& lay = part.zlay;
@@ -438,15 +453,23 @@ int gbntt_batch_execute_host(gbntt_batch* b, const void* const* h_in, void* cons
             std::vector<SegDev> segs = lay.segs;
             for (size_t j = 0; j < segs.size(); ++j) {
                 const int k = part.user_index[j];
-                segs[j].a.in = gbntt_internal_mapped(h_in[k]);
-                segs[j].a.out = const_cast<void*>(gbntt_internal_mapped(h_out[k]));
+                segs[j].a.in = mapped_in[k];
+                segs[j].a.out = const_cast<void*>(mapped_out[k]);
             }
-            cudaError_t e = cudaMemcpyAsync(lay.d_segs, segs.data(), sizeof(SegDev) * segs.size(),
-                                            cudaMemcpyHostToDevice, s);
-            if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("descriptors: ") + cudaGetErrorString(e));
+            // the same host buffers as the previous call (every earlier call
+            // synchronised its stream): the device descriptors are current
+            cudaError_t e = cudaSuccess;
+            if (lay.live.size() != segs.size() ||
+                std::memcmp(lay.live.data(), segs.data(), sizeof(SegDev) * segs.size()) != 0) {
+                lay.live.clear();
+                e = cudaMemcpyAsync(lay.d_segs, segs.data(), sizeof(SegDev) * segs.size(), cudaMemcpyHostToDevice, s);
+                if (e != cudaSuccess)
+                    return batch_fail(GBNTT_ERR_CUDA, std::string("descriptors: ") + cudaGetErrorString(e));
+                uploaded[i] = std::move(segs);
+            }
             BatchDev bd;
             bd.segs = lay.d_segs;
-            bd.nsegs = (int)segs.size();
+            bd.nsegs = (int)lay.segs.size();
             bd.total_tiles = lay.total_tiles;
             bd.ctr = b->d_ctr + CTR_WORDS * (2 + i);
             int sb = lay.stage_bytes;
@@ -468,6 +491,8 @@ int gbntt_batch_execute_host(gbntt_batch* b, const void* const* h_in, void* cons
         }
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("synchronize: ") + cudaGetErrorString(e));
+        for (int i = 0; i < b->nparts; ++i)
+            if (!uploaded[i].empty()) b->parts[i].zlay.live = std::move(uploaded[i]);
         return GBNTT_OK;
     }
     for (size_t k = 0; k < b->user.size(); ++k) {

@@ -297,6 +297,34 @@ def test_batch_execute_host_zero_copy(gb):
     assert all(np.array_equal(a, b) for a, b in zip(page_out, want))
 
 
+def test_zero_copy_buffer_switches(gb):
+    """Zero-copy calls alternating between two sets of pinned buffers (A, B, A,
+    B with different inputs): each call transforms the buffers it is given,
+    so device descriptors reused from the previous call stay correct."""
+    rng = np.random.default_rng(SEED + 101)
+    specs = [(2, 1024, 12289, np.int16), (4, 4096, 998244353, np.int32)]
+    plans = [gb.Plan(k, n, q, root_for(q, n)) for k, n, q, _ in specs]
+    sets = []
+    for _ in range(2):
+        xs = [rng.integers(0, q, (19, n)).astype(dt) for _, n, q, dt in specs]
+        want = [p(torch.from_numpy(x).cuda()).cpu().numpy() for p, x in zip(plans, xs)]
+        ins = [torch.from_numpy(x).pin_memory() for x in xs]
+        outs = [torch.empty_like(t).pin_memory() for t in ins]
+        sets.append((ins, outs, want))
+    batch = gb.Batch([(p, torch.from_numpy(x.numpy()).cuda(), torch.empty_like(torch.from_numpy(x.numpy())).cuda())
+                      for p, x in zip(plans, sets[0][0])])
+    for rep in range(4):
+        ins, outs, want = sets[rep % 2]
+        for t in outs:
+            t.zero_()
+        batch.execute_host(ins, outs)
+        assert all(np.array_equal(o.numpy(), w) for o, w in zip(outs, want)), rep
+        for t in outs:
+            t.zero_()
+        plans[0].execute_host(ins[0], outs[0])
+        assert np.array_equal(outs[0].numpy(), want[0]), rep
+
+
 # ---------------------------------------------------------------------------
 # fused bit reversal (natural order) and fused n^-1 epilogue
 # ---------------------------------------------------------------------------
