@@ -221,9 +221,6 @@ __host__ __device__ constexpr int r8_stage_offset(int L, int s) {
     return o;
 }
 
-// padded shared-memory index of a position (one spare word every 32)
-__device__ __forceinline__ int spad(int pos) { return pos + (pos >> 5); }
-
 // shared-memory words per polynomial of the exchange buffer (16-byte
 // multiple): room for the padded exchange layouts below (at most one spare
 // word per 16 positions)
@@ -276,6 +273,42 @@ __host__ __device__ constexpr int scalar_degree(int L, int EL, int LOA, int LOB,
 }
 
 struct XPad { int s, t; };
+
+__host__ __device__ constexpr int brev_n(int x, int nb) {
+    int r = 0;
+    for (int i = 0; i < nb; ++i) r |= ((x >> i) & 1) << (nb - 1 - i);
+    return r;
+}
+
+// the same for the bit-reversal permutation of window LO: the register of
+// position p is written at bitrev(p) and read back at p
+__host__ __device__ constexpr int brev_degree(int L, int EL, int LO, int s, int t) {
+    const int G = 1 << (L - EL);
+    int total = 0;
+    for (int side = 0; side < 2; ++side) {
+        int cnt[32] = {};
+        int worst = 0;
+        for (int lane = 0; lane < 32; ++lane) {
+            const int p = posmap_c(LO, EL, lane % G, 0);
+            const int w = (lane / G) * xwords(L) + xpad(side ? p : brev_n(p, L), s, t);
+            const int c = ++cnt[w & 31];
+            worst = c > worst ? c : worst;
+        }
+        total += worst;
+    }
+    return total;
+}
+__host__ __device__ constexpr XPad brev_layout(int L, int EL, int LO) {
+    XPad best{5, 1};
+    int bd = brev_degree(L, EL, LO, 5, 1);
+    for (int s = 4; s <= L && bd > 2; ++s)
+        for (int t = 1; t <= 16 && bd > 2; t *= 2) {
+            if (t * 32 > (2 << s) || xpad((1 << L) - 1, s, t) >= xwords(L)) continue;
+            const int d = brev_degree(L, EL, LO, s, t);
+            if (d < bd) { bd = d; best = XPad{s, t}; }
+        }
+    return best;
+}
 
 // the padding of a scalar exchange: fewest conflicts, then the first candidate
 __host__ __device__ constexpr XPad scalar_layout(int L, int EL, int LOA, int LOB) {
@@ -610,15 +643,18 @@ __device__ __forceinline__ void permute_br(int (&v)[1 << EL], int* sp, int g) {
         for (int k = 0; k < E; ++k) v[k] = t[brev_c<L>(k)];
     } else {
         // the thread bits and the register bits of a position are disjoint, so
-        // bitrev(pos) = bitrev(thread part) | bitrev(register part), and spad
-        // splits the same way: one runtime base plus a constant per register
-        const int base = spad((int)(__brev((unsigned)posmap<LO, EL>(g, 0)) >> (32 - L)));
+        // bitrev(pos) = bitrev(thread part) | bitrev(register part), and the
+        // padding (chosen like an exchange's) splits the same way: one runtime
+        // base plus a constant per register
+        constexpr XPad X = brev_layout(L, EL, LO);
+        const int wb = xpad((int)(__brev((unsigned)posmap<LO, EL>(g, 0)) >> (32 - L)), X.s, X.t);
         group_sync<G>();
 #pragma unroll
-        for (int k = 0; k < E; ++k) sp[base + spad(brev_c<L>(k << LO))] = v[k];
+        for (int k = 0; k < E; ++k) sp[wb + xpad(brev_c<L>(k << LO), X.s, X.t)] = v[k];
         group_sync<G>();
+        const int rb = xpad(posmap<LO, EL>(g, 0), X.s, X.t);
 #pragma unroll
-        for (int k = 0; k < E; ++k) v[k] = sp[spad(posmap<LO, EL>(g, k))];
+        for (int k = 0; k < E; ++k) v[k] = sp[rb + xpad(k << LO, X.s, X.t)];
     }
 }
 
