@@ -306,7 +306,9 @@ int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t
     a.fb_fs = hp.fb_fs;
     a.fb_wq = hp.fb_wq;
     a.r8_sym = hp.r8_sym;
-    a.tail_wq = hp.tail_wq;
+    // radix-8: the multiplier of the twiddle 1, also for the k = 0 outputs of
+    // every stage (table entry 0 is that twiddle, in the plan's w' mode)
+    a.tail_wq = (p->fam == F_R8F16 && hp.tab.size() >= 2) ? hp.tab[1] : hp.tail_wq;
     for (int i = 0; i < 64; ++i) a.f8[i] = hp.f8[i];
     for (int i = 0; i < 4; ++i) a.f8s[i] = hp.f8s[i];
     for (int i = 0; i < 16; ++i) a.ftail[i] = hp.ftail[i];

@@ -43,7 +43,7 @@ struct KArgs {
     int scale;            // inverse designs: full Barrett multiplication by n^-1 fused into the store
     int fb_fs, fb_wq;     // its signed factor and multiplier
     int r8_sym;           // radix-8 matrix symmetric: use the factored butterfly
-    int tail_wq;          // radix-8 tail stage multiplier of the twiddle 1
+    int tail_wq;          // radix-8: multiplier of the twiddle 1 (output 0 of every stage, the tail stage)
     int f8[64];           // radix-8 matrix [m][k]
     int f8s[4];           // f1, f2, f3
     int ftail[16];        // tail matrix [m][k]
@@ -588,8 +588,10 @@ __device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const
                         y[k] = acc;
                     }
                 }
+                // output 0 has the twiddle 1 in every stage: its multiplier is an argument
+                v[k0] = r8red(y[0], 1, a.tail_wq, q);
 #pragma unroll
-                for (int k = 0; k < 8; ++k) {
+                for (int k = 1; k < 8; ++k) {
                     const int2 t = __ldg(&a.tab[OFF + (k << B) + rr]);
                     v[k0 | (brev_c<3>(k) << KB)] = r8red(y[k], t.x, t.y, q);
                 }
