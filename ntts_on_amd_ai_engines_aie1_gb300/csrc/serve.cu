@@ -175,16 +175,25 @@ struct Group {                  // one plan's requests in one micro-batch
 
 struct Slot {
     cudaStream_t stream = nullptr;
+    cudaStream_t aux = nullptr;            // the int32 persistent launch, beside the int16 one
     cudaEvent_t done = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     bool busy = false;
     std::vector<Group> groups;
-    CopyDesc* h_desc = nullptr;   // page-locked descriptor table: gather copies, then scatter copies
-    CopyDesc* d_desc = nullptr;
-    SegDev* h_seg = nullptr;      // page-locked segment descriptors: int16 part, then int32 part
-    SegDev* d_seg = nullptr;
+    // page-locked descriptor block of one micro-batch: the gather copies, the
+    // scatter copies (the last one returns the error words), then the segment
+    // descriptors of the int16 and the int32 persistent launches; it goes to
+    // d_blk with one copy
+    unsigned char* h_blk = nullptr;
+    unsigned char* d_blk = nullptr;
     unsigned long long* d_ctr = nullptr;   // tile counters of the two persistent launches
-    unsigned long long* h_err = nullptr;   // their error words, read back with the results
+    unsigned long long* h_err = nullptr;   // their error words (mapped), written by the scatter kernel
+    unsigned long long* m_err = nullptr;   // device address of h_err
 };
+
+constexpr size_t ERR_BYTES = 2 * CTR_WORDS * sizeof(unsigned long long);
+constexpr size_t BLK_ALIGN = 128;
+size_t blk_round(size_t b) { return (b + BLK_ALIGN - 1) / BLK_ALIGN * BLK_ALIGN; }
 
 // a plan as the persistent kernel sees it
 struct PlanInfo {
@@ -272,18 +281,21 @@ void finish_slot(gbntt_server* s, Slot& sl) {
     s->cv_done.notify_all();
 }
 
-// Issue one micro-batch on slot sl: gather (kernel for mapped requests, copy
-// engine for the others), one in-place launch per plan group, scatter, event.
+// Issue one micro-batch on slot sl: one descriptor upload, the gather kernel
+// for mapped requests (copy engine for the others), the int16 and int32
+// persistent launches side by side, the plans' own launches, the scatter
+// kernel (which also returns the persistent launches' error words), event.
 int issue(gbntt_server* s, Slot& sl) {
     uint64_t nl = 0;   // launches of this micro-batch (published under the lock at the end)
+    CopyDesc* desc = reinterpret_cast<CopyDesc*>(sl.h_blk);
     int nin = 0;
     unsigned long long cin = 0;
     for (auto& g : sl.groups) {               // gather descriptors
         size_t at = 0;
         for (auto& r : g.reqs) {
             if (r.m_in) {
-                sl.h_desc[nin++] = CopyDesc{static_cast<const unsigned char*>(r.m_in),
-                                            reinterpret_cast<unsigned char*>(s->d_arena + g.off + at), r.bytes, cin};
+                desc[nin++] = CopyDesc{static_cast<const unsigned char*>(r.m_in),
+                                       reinterpret_cast<unsigned char*>(s->d_arena + g.off + at), r.bytes, cin};
                 cin += (r.bytes + COPY_CHUNK - 1) / COPY_CHUNK;
             }
             at += r.bytes;
@@ -291,7 +303,7 @@ int issue(gbntt_server* s, Slot& sl) {
     }
     int nout = 0;
     unsigned long long cout = 0;
-    CopyDesc* od = sl.h_desc + nin;
+    CopyDesc* od = desc + nin;
     for (auto& g : sl.groups) {               // scatter descriptors
         size_t at = 0;
         for (auto& r : g.reqs) {
@@ -303,14 +315,48 @@ int issue(gbntt_server* s, Slot& sl) {
             at += r.bytes;
         }
     }
-    cudaError_t e;
-    if (nin + nout) {
-        e = cudaMemcpyAsync(sl.d_desc, sl.h_desc, (size_t)(nin + nout) * sizeof(CopyDesc), cudaMemcpyHostToDevice,
-                            sl.stream);
-        if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve descriptors: ") + cudaGetErrorString(e));
+    od[nout++] = CopyDesc{reinterpret_cast<const unsigned char*>(sl.d_ctr),
+                          reinterpret_cast<unsigned char*>(sl.m_err), ERR_BYTES, cout};
+    cout += 1;
+
+    // segment descriptors, one persistent launch per storage type, largest n first
+    std::vector<const Group*> order;
+    for (auto& g : sl.groups) order.push_back(&g);
+    std::stable_sort(order.begin(), order.end(), [&](const Group* x, const Group* y) {
+        return s->pinfo[x->plan].L > s->pinfo[y->plan].L;
+    });
+    int nseg[2] = {0, 0};
+    for (const Group* g : order)
+        if (s->pinfo[g->plan].part >= 0) ++nseg[s->pinfo[g->plan].part];
+    const size_t seg_off = blk_round((size_t)(nin + nout) * sizeof(CopyDesc));
+    SegDev* segs = reinterpret_cast<SegDev*>(sl.h_blk + seg_off);
+    int fill[2] = {0, nseg[0]};
+    long long tiles[2] = {0, 0};
+    for (const Group* g : order) {
+        const PlanInfo& pi = s->pinfo[g->plan];
+        if (pi.part < 0) continue;
+        SegDev& sd = segs[fill[pi.part]++];
+        std::memset(&sd, 0, sizeof(sd));
+        sd.a = pi.a;
+        sd.a.in = s->d_arena + g->off;
+        sd.a.out = s->d_arena + g->off;
+        sd.a.batch = (long long)g->count;
+        sd.n = 1 << pi.L;
+        sd.elem_bytes = pi.eb;
+        sd.variant = variant_id(pi.fam, pi.L);
+        sd.polys_per_tile = BATCH_CTA >> (pi.L - batch_el(pi.L, s->part[pi.part].cfg->elmax));
+        sd.tiles = (sd.a.batch + sd.polys_per_tile - 1) / sd.polys_per_tile;
+        sd.tile0 = tiles[pi.part];
+        tiles[pi.part] += sd.tiles;
     }
+    const size_t used = seg_off + (size_t)(nseg[0] + nseg[1]) * sizeof(SegDev);
+    cudaError_t e = cudaMemcpyAsync(sl.d_blk, sl.h_blk, used, cudaMemcpyHostToDevice, sl.stream);
+    if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve descriptors: ") + cudaGetErrorString(e));
+    const CopyDesc* d_desc = reinterpret_cast<const CopyDesc*>(sl.d_blk);
+    SegDev* d_segs = reinterpret_cast<SegDev*>(sl.d_blk + seg_off);
+
     if (nin) {
-        k_copy_desc<<<(unsigned)cin, COPY_THREADS, 0, sl.stream>>>(sl.d_desc, nin);
+        k_copy_desc<<<(unsigned)cin, COPY_THREADS, 0, sl.stream>>>(d_desc, nin);
         gbntt_internal_count_launch();
         ++nl;
     }
@@ -325,69 +371,46 @@ int issue(gbntt_server* s, Slot& sl) {
             at += r.bytes;
         }
     }
-    // one persistent launch per storage type over all groups, largest n first
-    {
-        std::vector<const Group*> order;
-        for (auto& g : sl.groups) order.push_back(&g);
-        std::stable_sort(order.begin(), order.end(), [&](const Group* x, const Group* y) {
-            return s->pinfo[x->plan].L > s->pinfo[y->plan].L;
-        });
-        const int cap = (int)s->plans.size();
-        int nseg[2] = {0, 0};
-        long long tiles[2] = {0, 0};
-        for (const Group* g : order) {
-            const PlanInfo& pi = s->pinfo[g->plan];
-            if (pi.part < 0) continue;
-            SegDev& sd = sl.h_seg[pi.part * cap + nseg[pi.part]++];
-            std::memset(&sd, 0, sizeof(sd));
-            sd.a = pi.a;
-            sd.a.in = s->d_arena + g->off;
-            sd.a.out = s->d_arena + g->off;
-            sd.a.batch = (long long)g->count;
-            sd.n = 1 << pi.L;
-            sd.elem_bytes = pi.eb;
-            sd.variant = variant_id(pi.fam, pi.L);
-            sd.polys_per_tile = BATCH_CTA >> (pi.L - batch_el(pi.L, s->part[pi.part].cfg->elmax));
-            sd.tiles = (sd.a.batch + sd.polys_per_tile - 1) / sd.polys_per_tile;
-            sd.tile0 = tiles[pi.part];
-            tiles[pi.part] += sd.tiles;
-        }
-        for (int p = 0; p < 2; ++p) {
-            if (!nseg[p]) continue;
-            e = cudaMemcpyAsync(sl.d_seg + p * cap, sl.h_seg + p * cap, sizeof(SegDev) * nseg[p],
-                                cudaMemcpyHostToDevice, sl.stream);
-            if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve segments: ") + cudaGetErrorString(e));
-            const PartCfg& pc = s->part[p];
-            BatchDev bd;
-            bd.segs = sl.d_seg + p * cap;
-            bd.nsegs = nseg[p];
-            bd.total_tiles = tiles[p];
-            bd.ctr = sl.d_ctr + CTR_WORDS * p;
-            int sb = pc.stage;
-            void* args[] = {&bd, &sb};
-            const unsigned grid = (unsigned)std::min<long long>(pc.grid, tiles[p]);
-            e = cudaLaunchKernel(pc.cfg->fn, dim3(grid), dim3(BATCH_CTA), args, pc.smem, sl.stream);
-            if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve launch: ") + cudaGetErrorString(e));
+    auto launch_part = [&](int p, cudaStream_t st) -> cudaError_t {
+        const PartCfg& pc = s->part[p];
+        BatchDev bd;
+        bd.segs = d_segs + (p ? nseg[0] : 0);
+        bd.nsegs = nseg[p];
+        bd.total_tiles = tiles[p];
+        bd.ctr = sl.d_ctr + CTR_WORDS * p;
+        int sb = pc.stage;
+        void* args[] = {&bd, &sb};
+        const unsigned grid = (unsigned)std::min<long long>(pc.grid, tiles[p]);
+        const cudaError_t le = cudaLaunchKernel(pc.cfg->fn, dim3(grid), dim3(BATCH_CTA), args, pc.smem, st);
+        if (le == cudaSuccess) {
             gbntt_internal_count_launch();
             ++nl;
         }
-        for (const Group* g : order) {
-            if (s->pinfo[g->plan].part >= 0) continue;
-            const int rc = gbntt_execute(s->plans[g->plan], s->d_arena + g->off, s->d_arena + g->off, g->count,
-                                         sl.stream);
-            if (rc != GBNTT_OK) return rc;
-            ++nl;
-        }
-        // the persistent launches' error words come back with the results
-        e = cudaMemcpyAsync(sl.h_err, sl.d_ctr, 2 * CTR_WORDS * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                            sl.stream);
-        if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve status: ") + cudaGetErrorString(e));
+        return le;
+    };
+    if (nseg[0] && nseg[1]) {
+        // the two launches share nothing but the gather before them
+        e = cudaEventRecord(sl.fork, sl.stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(sl.aux, sl.fork, 0);
+        if (e == cudaSuccess) e = launch_part(1, sl.aux);
+        if (e == cudaSuccess) e = cudaEventRecord(sl.join, sl.aux);
+        if (e == cudaSuccess) e = launch_part(0, sl.stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(sl.stream, sl.join, 0);
+    } else {
+        for (int p = 0; p < 2 && e == cudaSuccess; ++p)
+            if (nseg[p]) e = launch_part(p, sl.stream);
     }
-    if (nout) {
-        k_copy_desc<<<(unsigned)cout, COPY_THREADS, 0, sl.stream>>>(sl.d_desc + nin, nout);
-        gbntt_internal_count_launch();
+    if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve launch: ") + cudaGetErrorString(e));
+    for (const Group* g : order) {
+        if (s->pinfo[g->plan].part >= 0) continue;
+        const int rc = gbntt_execute(s->plans[g->plan], s->d_arena + g->off, s->d_arena + g->off, g->count,
+                                     sl.stream);
+        if (rc != GBNTT_OK) return rc;
         ++nl;
     }
+    k_copy_desc<<<(unsigned)cout, COPY_THREADS, 0, sl.stream>>>(d_desc + nin, nout);
+    gbntt_internal_count_launch();
+    ++nl;
     for (auto& g : sl.groups) {
         char* base = s->d_arena + g.off;
         size_t at = 0;
@@ -620,20 +643,23 @@ int gbntt_server_create(gbntt_server** out, const gbntt_plan* const* plans, uint
     s->slots.resize(nslots);
     for (auto& sl : s->slots) {
         cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+        cudaStreamCreateWithFlags(&sl.aux, cudaStreamNonBlocking);
         cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
-        const size_t db = 2 * (size_t)s->max_group_requests * sizeof(CopyDesc);
-        const size_t sb = 2 * s->plans.size() * sizeof(SegDev);
-        const size_t cb = 2 * CTR_WORDS * sizeof(unsigned long long);
-        if (cudaHostAlloc(&sl.h_desc, db, cudaHostAllocDefault) != cudaSuccess ||
-            cudaMalloc(&sl.d_desc, db) != cudaSuccess ||
-            cudaHostAlloc(&sl.h_seg, sb, cudaHostAllocDefault) != cudaSuccess ||
-            cudaMalloc(&sl.d_seg, sb) != cudaSuccess ||
-            cudaHostAlloc(&sl.h_err, cb, cudaHostAllocDefault) != cudaSuccess ||
-            cudaMalloc(&sl.d_ctr, cb) != cudaSuccess || cudaMemset(sl.d_ctr, 0, cb) != cudaSuccess) {
+        cudaEventCreateWithFlags(&sl.fork, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&sl.join, cudaEventDisableTiming);
+        // gather + scatter copies of every request, the error-word copy, the segments
+        const size_t bb = blk_round((2 * (size_t)s->max_group_requests + 1) * sizeof(CopyDesc)) +
+                          2 * s->plans.size() * sizeof(SegDev);
+        if (cudaHostAlloc(&sl.h_blk, bb, cudaHostAllocDefault) != cudaSuccess ||
+            cudaMalloc(&sl.d_blk, bb) != cudaSuccess ||
+            cudaHostAlloc(&sl.h_err, ERR_BYTES, cudaHostAllocMapped) != cudaSuccess ||
+            cudaHostGetDevicePointer(reinterpret_cast<void**>(&sl.m_err), sl.h_err, 0) != cudaSuccess ||
+            cudaMalloc(&sl.d_ctr, ERR_BYTES) != cudaSuccess || cudaMemset(sl.d_ctr, 0, ERR_BYTES) != cudaSuccess) {
             cudaGetLastError();
             gbntt_server_destroy(s);
             return sfail(GBNTT_ERR_NOMEM, "descriptor tables allocation failed");
         }
+        std::memset(sl.h_err, 0, ERR_BYTES);
     }
     s->t_first = s->t_last = Clock::now();
     s->worker = std::thread(worker_main, s);
@@ -748,11 +774,12 @@ int gbntt_server_destroy(gbntt_server* s) {
     for (auto& sl : s->slots) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
         if (sl.done) cudaEventDestroy(sl.done);
+        if (sl.fork) cudaEventDestroy(sl.fork);
+        if (sl.join) cudaEventDestroy(sl.join);
         if (sl.stream) cudaStreamDestroy(sl.stream);
-        if (sl.h_desc) cudaFreeHost(sl.h_desc);
-        if (sl.d_desc) cudaFree(sl.d_desc);
-        if (sl.h_seg) cudaFreeHost(sl.h_seg);
-        if (sl.d_seg) cudaFree(sl.d_seg);
+        if (sl.aux) cudaStreamDestroy(sl.aux);
+        if (sl.h_blk) cudaFreeHost(sl.h_blk);
+        if (sl.d_blk) cudaFree(sl.d_blk);
         if (sl.h_err) cudaFreeHost(sl.h_err);
         if (sl.d_ctr) cudaFree(sl.d_ctr);
     }
