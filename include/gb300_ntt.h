@@ -110,11 +110,13 @@ int gbntt_execute(const gbntt_plan* plan, const void* d_in, void* d_out, uint64_
  * both buffers are page-locked and mapped into the device's address space
  * (cudaHostAlloc / cudaHostRegister memory, 16-byte aligned) and the design
  * has a persistent-kernel form (all but the radix-4 inverse, the radix-8
- * stage, the bit-reversal and full Barrett units and int32 n >= 2^16), the
+ * stage, the bit-reversal and full Barrett units and int32 n >= 2^14), the
  * zero-copy persistent kernel reads and writes them directly over the
  * host-device link; its scratch (a descriptor and tile counters) is allocated
- * on the first such call.  Otherwise the inputs are copied to device staging
- * memory owned by the plan, transformed and copied back. */
+ * on the first such call, and a call on the same buffers and count as the
+ * previous one reuses the descriptor already on the device.  Otherwise the
+ * inputs are copied to device staging memory owned by the plan, transformed
+ * and copied back. */
 int gbntt_execute_host(gbntt_plan* plan, const void* h_in, void* h_out, uint64_t batch,
                        void* stream);
 
@@ -169,8 +171,10 @@ int gbntt_batch_graph_launch(gbntt_batch* batch, void* stream);
  * address space (cudaHostAlloc / cudaHostRegister memory, 16-byte aligned),
  * the zero-copy form of the persistent kernel reads and writes them directly
  * over the host-device link, so inbound and outbound traffic overlap (one
- * launch per storage type; h_in[i] == h_out[i] allowed); the other segments
- * are copied through their device buffers.  Otherwise copies h_in[i] into
+ * launch per storage type; h_in[i] == h_out[i] allowed; a call on the same
+ * buffers as the previous successful one reuses the descriptors already on
+ * the device); the other segments are copied through their device buffers.
+ * Otherwise copies h_in[i] into
  * segment i's device input, runs the batch (graph replay) and copies every
  * segment's device output to h_out[i].  Not concurrent with other launches of
  * the same batch. */
