@@ -348,7 +348,10 @@ def run_ours(args):
                      "frac": achieved / peak, "peak_source": peak_src,
                      "kernel": "k_batch<int16> persistent radix-4 (all 16384 polys per launch)",
                      "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_ms": ms,
-                     "traffic": (traffic or {}).get("bytes_per_launch")},
+                     "traffic": (traffic or {}).get("bytes_per_launch"),
+                     # the bound that holds: integer issue (ncu capture of the same kernel)
+                     "issue": {k: (traffic or {}).get(k) for k in
+                               ("issue_active_frac", "alu_pipe_frac", "thread_instructions_per_coefficient")}},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": launches,
