@@ -255,15 +255,25 @@ __device__ __forceinline__ int posmap(int g, int k) { return posmap_c(LO, EL, g,
 
 __host__ __device__ constexpr int xpad(int p, int s, int t) { return p + (p >> s) * t; }
 
-// bank-conflict degree summed over both sides (2 = conflict free)
-__host__ __device__ constexpr int scalar_degree(int L, int EL, int LOA, int LOB, int s, int t) {
+__host__ __device__ constexpr int brev_n(int x, int nb) {
+    int r = 0;
+    for (int i = 0; i < nb; ++i) r |= ((x >> i) & 1) << (nb - 1 - i);
+    return r;
+}
+
+// Bank-conflict degree of a padded layout, summed over the writing side
+// (window LOA, at bit-reversed positions when BRA) and the reading side
+// (window LOB): 2 = conflict free.
+__host__ __device__ constexpr int pad_degree(int L, int EL, int LOA, bool BRA, int LOB, int s, int t) {
     const int G = 1 << (L - EL);
     int total = 0;
     for (int side = 0; side < 2; ++side) {
         int cnt[32] = {};
         int worst = 0;
         for (int lane = 0; lane < 32; ++lane) {
-            const int w = (lane / G) * xwords(L) + xpad(posmap_c(side ? LOB : LOA, EL, lane % G, 0), s, t);
+            int p = posmap_c(side ? LOB : LOA, EL, lane % G, 0);
+            if (!side && BRA) p = brev_n(p, L);
+            const int w = (lane / G) * xwords(L) + xpad(p, s, t);
             const int c = ++cnt[w & 31];
             worst = c > worst ? c : worst;
         }
@@ -274,54 +284,26 @@ __host__ __device__ constexpr int scalar_degree(int L, int EL, int LOA, int LOB,
 
 struct XPad { int s, t; };
 
-__host__ __device__ constexpr int brev_n(int x, int nb) {
-    int r = 0;
-    for (int i = 0; i < nb; ++i) r |= ((x >> i) & 1) << (nb - 1 - i);
-    return r;
-}
-
-// the same for the bit-reversal permutation of window LO: the register of
-// position p is written at bitrev(p) and read back at p
-__host__ __device__ constexpr int brev_degree(int L, int EL, int LO, int s, int t) {
-    const int G = 1 << (L - EL);
-    int total = 0;
-    for (int side = 0; side < 2; ++side) {
-        int cnt[32] = {};
-        int worst = 0;
-        for (int lane = 0; lane < 32; ++lane) {
-            const int p = posmap_c(LO, EL, lane % G, 0);
-            const int w = (lane / G) * xwords(L) + xpad(side ? p : brev_n(p, L), s, t);
-            const int c = ++cnt[w & 31];
-            worst = c > worst ? c : worst;
-        }
-        total += worst;
-    }
-    return total;
-}
-__host__ __device__ constexpr XPad brev_layout(int L, int EL, int LO) {
+// the padding with the fewest conflicts (the first such candidate, one spare
+// word every 32 positions first) that fits xwords(L)
+__host__ __device__ constexpr XPad pad_layout(int L, int EL, int LOA, bool BRA, int LOB) {
     XPad best{5, 1};
-    int bd = brev_degree(L, EL, LO, 5, 1);
+    int bd = pad_degree(L, EL, LOA, BRA, LOB, 5, 1);
     for (int s = 4; s <= L && bd > 2; ++s)
         for (int t = 1; t <= 16 && bd > 2; t *= 2) {
             if (t * 32 > (2 << s) || xpad((1 << L) - 1, s, t) >= xwords(L)) continue;
-            const int d = brev_degree(L, EL, LO, s, t);
+            const int d = pad_degree(L, EL, LOA, BRA, LOB, s, t);
             if (d < bd) { bd = d; best = XPad{s, t}; }
         }
     return best;
 }
-
-// the padding of a scalar exchange: fewest conflicts, then the first candidate
+// a scalar exchange from window LOA to window LOB
 __host__ __device__ constexpr XPad scalar_layout(int L, int EL, int LOA, int LOB) {
-    XPad best{5, 1};
-    int bd = scalar_degree(L, EL, LOA, LOB, 5, 1);
-    for (int s = 4; s <= L && bd > 2; ++s)
-        for (int t = 1; t <= 16 && bd > 2; t *= 2) {
-            if (t * 32 > (2 << s) || xpad((1 << L) - 1, s, t) >= xwords(L)) continue;
-            const int d = scalar_degree(L, EL, LOA, LOB, s, t);
-            if (d < bd) { bd = d; best = XPad{s, t}; }
-        }
-    return best;
+    return pad_layout(L, EL, LOA, false, LOB);
 }
+// the bit-reversal permutation of window LO: the register of position p is
+// written at bitrev(p) and read back at p
+__host__ __device__ constexpr XPad brev_layout(int L, int EL, int LO) { return pad_layout(L, EL, LO, true, LO); }
 
 __host__ __device__ constexpr int vchunk(int pos, int OLO, int VB) {
     return ((pos >> (OLO + VB)) << OLO) | (pos & ((1 << OLO) - 1));
