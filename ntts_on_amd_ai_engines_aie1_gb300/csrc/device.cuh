@@ -44,6 +44,7 @@ struct KArgs {
     int fb_fs, fb_wq;     // its signed factor and multiplier
     int r8_sym;           // radix-8 matrix symmetric: use the factored butterfly
     int tail_wq;          // radix-8: multiplier of the twiddle 1 (output 0 of every stage, the tail stage)
+    int tab_bytes;        // per-plan launch: table bytes to prefetch into L1 first (0: none)
     int f8[64];           // radix-8 matrix [m][k]
     int f8s[4];           // f1, f2, f3
     int ftail[16];        // tail matrix [m][k]
@@ -741,6 +742,14 @@ __device__ __forceinline__ void k_ntt_body(const KArgs& a) {
     int v[1 << EL];
     constexpr int LO0 = window_lo(FAM, L, EL, 0);
     constexpr int LOZ = window_lo(FAM, L, EL, NS - 1);
+    // Every stage's table loads sit on the transform's dependent path; in a
+    // launch of a few polynomials (latency) they would wait stage by stage, so
+    // the host asks for the whole table in L1 first, beside the polynomial's load.
+    {
+        const char* tb = a.tab16 ? reinterpret_cast<const char*>(a.tab16) : reinterpret_cast<const char*>(a.tab);
+        for (int off = tid * 128; off < a.tab_bytes; off += (int)blockDim.x * 128)
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(tb + off));
+    }
     if (active) {
         load_poly<I32, L, EL, LO0>(v, a, poly, g);
     } else {
