@@ -23,6 +23,7 @@ struct gbntt_plan {
     int fam = -1;          // transform family of k_ntt, -1 for the single-purpose kernels
     bool br = false;       // bit-reversed load and store (radix-4 inverse)
     KernelInfo ki;
+    KernelInfo kl;         // latency form for launches of at most one CTA per SM (fn nullptr: none)
     LargeInfo large;       // int32 n >= 2^16: two-pass schedule (large.cols != nullptr)
     KArgs base;            // constants shared by every launch
     int2* d_tab = nullptr;
@@ -62,14 +63,14 @@ int family_of(int kind) {
     }
 }
 
-KernelInfo kernel_for(int fam, int L, bool br) {
+KernelInfo kernel_for(int fam, int L, bool br, bool lat) {
     switch (fam) {
-    case F_R2F16: return kinfo_r2f16(L);
-    case F_R2I16: return kinfo_r2i16(L);
-    case F_R4F16: return kinfo_r4(L, br);
-    case F_R8F16: return kinfo_r8(L);
-    case F_R2F32: return kinfo_r2f32(L);
-    case F_R2G32: return kinfo_r2g32(L);
+    case F_R2F16: return kinfo_r2f16(L, lat);
+    case F_R2I16: return kinfo_r2i16(L, lat);
+    case F_R4F16: return kinfo_r4(L, br, lat);
+    case F_R8F16: return kinfo_r8(L, lat);
+    case F_R2F32: return kinfo_r2f32(L, lat);
+    case F_R2G32: return kinfo_r2g32(L, lat);
     default: return KernelInfo();
     }
 }
@@ -120,20 +121,24 @@ int launch(const gbntt_plan* p, const void* d_in, void* d_out, uint64_t batch, c
         }
         return GBNTT_OK;
     } else if (p->fam >= 0) {
-        const unsigned long long blocks = (batch + p->ki.polys - 1) / p->ki.polys;
-        if (blocks > 0x7FFFFFFFull) return fail(GBNTT_ERR_ARG, "batch too large for one launch");
-        // A launch of at most one CTA per SM is latency-bound: its CTAs pull
-        // the table into L1 up front (a large launch finds it there already,
-        // and the extra prefetches measured 6-8 % slower for int32 and radix-8).
+        // A launch of at most one CTA per SM is latency-bound: it takes the
+        // latency form (one polynomial per CTA over up to 256 threads) where
+        // the design has one, and its CTAs pull the table into L1 up front (a
+        // large launch finds it there already, and the extra prefetches
+        // measured 6-8 % slower for int32 and radix-8).
         static const int sms = [] {
             int dev = 0, n = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
             return n > 0 ? n : 1;
         }();
+        const bool small = batch <= (uint64_t)sms;
+        const KernelInfo& k = small && p->kl.fn ? p->kl : p->ki;
+        const unsigned long long blocks = (batch + k.polys - 1) / k.polys;
+        if (blocks > 0x7FFFFFFFull) return fail(GBNTT_ERR_ARG, "batch too large for one launch");
         a.tab_bytes = blocks <= (unsigned long long)sms ? (int)p->tab_bytes : 0;
         void* args[] = {&a};
-        e = cudaLaunchKernel(p->ki.fn, dim3((unsigned)blocks), dim3(p->ki.threads), args, p->ki.smem, s);
+        e = cudaLaunchKernel(k.fn, dim3((unsigned)blocks), dim3(k.threads), args, k.smem, s);
     } else if (p->hp.kind == K_R8_I16_STAGE) {
         e = launch_r8_stage(a, p->hp.L, s);
     } else if (p->hp.kind == K_BITREV_I16) {
@@ -239,7 +244,8 @@ int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t
             return fail(GBNTT_ERR_LENGTH, "no kernel for this length");
         }
     } else if (p->fam >= 0) {
-        p->ki = kernel_for(p->fam, hp.L, p->br);
+        p->ki = kernel_for(p->fam, hp.L, p->br, false);
+        p->kl = kernel_for(p->fam, hp.L, p->br, true);
         if (!p->ki.fn) {
             delete p;
             return fail(GBNTT_ERR_LENGTH, "no kernel for this length");

@@ -817,33 +817,46 @@ __host__ __device__ constexpr int choose_polys(int fam, int L) {
     const int p = 256 / G;
     return p < 1 ? 1 : p;
 }
-__host__ __device__ constexpr int smem_bytes(int fam, int L) {
-    return num_windows(fam, L, choose_el(fam, L)) > 1 ? choose_polys(fam, L) * xwords(L) * 4 : 0;
+
+// The latency form of a per-plan launch (a launch of at most one CTA per SM):
+// one polynomial per CTA spread over up to 256 threads, so each thread's
+// share of every stage is short; at least one butterfly step per window.
+// Measured for n = 1024 radix-2 int16, one polynomial, L2 flushed: forward +
+// inverse 17.5 -> 10.5 us against 16 (forward) / 32 (inverse) coefficients
+// per thread.
+__host__ __device__ constexpr int lat_el(int fam, int L) {
+    const int lo = fam == F_R8F16 ? 3 : 2;
+    return L - 8 > lo ? L - 8 : lo;
+}
+// the latency form exists where it differs from the throughput form
+__host__ __device__ constexpr bool has_lat(int fam, int L) {
+    return L >= 9 && L <= 12 && (lat_el(fam, L) != choose_el(fam, L) || choose_polys(fam, L) != 1);
 }
 
-template <int FAM, int L, bool BR>
+template <int FAM, int L, bool BR, bool LAT = false>
 KernelInfo make_kernel_info() {
-    constexpr int EL = choose_el(FAM, L);
-    constexpr int P = choose_polys(FAM, L);
+    constexpr int EL = LAT ? lat_el(FAM, L) : choose_el(FAM, L);
+    constexpr int P = LAT ? 1 : choose_polys(FAM, L);
     KernelInfo ki;
     if constexpr (kntt_two_ctas(FAM, P << (L - EL)))
         ki.fn = reinterpret_cast<const void*>(&k_ntt2<FAM, L, EL, P, BR>);
     else
         ki.fn = reinterpret_cast<const void*>(&k_ntt<FAM, L, EL, P, BR>);
     ki.threads = P << (L - EL);
-    ki.smem = smem_bytes(FAM, L);
+    ki.smem = num_windows(FAM, L, EL) > 1 ? P * xwords(L) * 4 : 0;
     ki.polys = P;
     ki.el = EL;
     return ki;
 }
 
 // kernel tables, one per family (kernels_*.cu)
-KernelInfo kinfo_r2f16(int L);
-KernelInfo kinfo_r2i16(int L);
-KernelInfo kinfo_r2f32(int L);
-KernelInfo kinfo_r2g32(int L);
-KernelInfo kinfo_r4(int L, bool br);
-KernelInfo kinfo_r8(int L);
+// lat: the latency form (an empty KernelInfo where the design has none)
+KernelInfo kinfo_r2f16(int L, bool lat);
+KernelInfo kinfo_r2i16(int L, bool lat);
+KernelInfo kinfo_r2f32(int L, bool lat);
+KernelInfo kinfo_r2g32(int L, bool lat);
+KernelInfo kinfo_r4(int L, bool br, bool lat);
+KernelInfo kinfo_r8(int L, bool lat);
 
 // two-pass schedule for int32 transforms longer than one CTA holds (kernels_large.cu)
 struct LargeInfo {

@@ -297,6 +297,27 @@ def test_batch_execute_host_zero_copy(gb):
     assert all(np.array_equal(a, b) for a, b in zip(page_out, want))
 
 
+FORM_CASES = [  # (kind, oracle kind, q, L, dtype, oracle options) -- designs with a latency form
+    (0, 0, 12289, 9, np.int16, {}), (0, 0, 12289, 10, np.int16, {}), (0, 0, 12289, 11, np.int16, {}),
+    (1, 1, 12289, 10, np.int16, {}), (1, 1, 12289, 12, np.int16, {}), (2, 2, 12289, 10, np.int16, {}),
+    (9, 9, 12289, 10, np.int16, {}), (8, 8, 12289, 10, np.int16, {"r8_exact": True}),
+    (8, 8, 12289, 11, np.int16, {"r8_exact": True}), (4, 4, 998244353, 9, np.int32, {}),
+    (4, 4, 998244353, 11, np.int32, {}), (5, 5, 998244353, 10, np.int32, {})]
+
+
+@pytest.mark.parametrize("kind,okind,q,L,dt,ok", FORM_CASES)
+def test_latency_and_throughput_forms(gb, orc, kind, okind, q, L, dt, ok):
+    """A per-plan launch of at most one CTA per SM takes the latency form (one
+    polynomial per CTA, up to 256 threads); a larger one the throughput form.
+    Both equal the oracle."""
+    n = 1 << L
+    root = root_for(q, n)
+    rng = np.random.default_rng(SEED + 300 + kind + L)
+    for batch in (1, 3, 400):
+        x = inputs(rng, batch, n, 0, q, dt)
+        check(gb, orc, kind, okind, n, q, root, x, oflags=ok)
+
+
 def test_zero_copy_buffer_switches(gb):
     """Zero-copy calls alternating between two sets of pinned buffers (A, B, A,
     B with different inputs): each call transforms the buffers it is given,
