@@ -28,7 +28,7 @@ struct Key {
 // (768-thread CTAs, one per SM, measured no faster on GB300.)
 constexpr Key kKeys[] = {
     {6, R4, 0}, {5, R4, 0}, {6, R2, 0}, {5, R2, 0}, {6, R8, 0}, {5, R8, 0}, {5, ALL16, 0},
-    {4, R4, 0}, {4, R4, 5}, {4, R4, 6}, {4, R2, 0}, {4, R2, 5}, {4, R8, 0}, {4, ALL16, 0},
+    {4, R4, 0}, {4, R4, 5}, {4, R4, 6}, {4, R2, 0}, {4, R2, 5}, {4, R8, 0}, {4, R8, 5}, {4, ALL16, 0},
 };
 constexpr int kN = (int)(sizeof(kKeys) / sizeof(kKeys[0]));
 BatchConfig kI16[kN];

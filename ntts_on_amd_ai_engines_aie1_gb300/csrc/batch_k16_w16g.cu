@@ -14,6 +14,7 @@ const void* batch_kernels_i16_w16g(int el, int set, int occ) {
 #define GB_K(EL, SET, OCC) \
     if (el == EL && set == SET && occ == OCC) return reinterpret_cast<const void*>(&k_batch<false, BATCH_CTA, EL, SET, OCC>);
     GB_K(4, R8, 0)
+    GB_K(4, R8, 5)
     GB_K(4, ALL16, 0)
 #undef GB_K
     return nullptr;
