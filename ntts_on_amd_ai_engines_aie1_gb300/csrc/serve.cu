@@ -587,11 +587,16 @@ int gbntt_server_create(gbntt_server** out, const gbntt_plan* const* plans, uint
             const BatchConfig* cfgs = nullptr;
             const int ncfg = p ? batch_configs_i32(&cfgs) : batch_configs_i16(&cfgs);
             // the narrowest covering configuration (16 coefficients per thread
-            // measured faster than 32 on mixed radix-4 batches)
+            // measured faster than 32 on mixed radix-4 batches), with the most
+            // resident CTAs among those
             const BatchConfig* cfg = nullptr;
+            auto resident = [&](const BatchConfig& c) {
+                return c.occ ? c.occ : batch_min_blocks(c.i32, c.cta, c.elmax);
+            };
             for (int c = 0; c < ncfg; ++c)
                 if (cfgs[c].cta == BATCH_CTA && (cfgs[c].set & mask) == mask && config_fits(cfgs[c], maxL) &&
-                    (!cfg || cfgs[c].elmax < cfg->elmax))
+                    (!cfg || cfgs[c].elmax < cfg->elmax ||
+                     (cfgs[c].elmax == cfg->elmax && resident(cfgs[c]) > resident(*cfg))))
                     cfg = &cfgs[c];
             if (!cfg) {   // no persistent kernel covers them: the plans launch on their own
                 for (auto& pi : s->pinfo)
