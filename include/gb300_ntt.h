@@ -214,7 +214,8 @@ int gbntt_batch_destroy(gbntt_batch* batch);
  * any stream capture.  Every call reuses the array and resets its counters, so
  * calls whose work overlaps on the GPU (different streams, no ordering
  * between them) race; serialise them on one stream.  No autotuning: the
- * configuration with 32 coefficients per thread is used. */
+ * narrowest compiled configuration covering the segments' designs and
+ * lengths, with the most resident CTAs among those, is used. */
 #define GBNTT_NOALLOC_MAX_SEGMENTS 16
 int gbntt_batch_execute_noalloc(const gbntt_segment* segs, uint32_t nsegs, void* stream);
 

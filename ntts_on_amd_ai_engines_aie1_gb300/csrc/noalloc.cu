@@ -110,12 +110,21 @@ extern "C" int gbntt_batch_execute_noalloc(const gbntt_segment* segs, uint32_t n
     size_t desc_off = 0;
     for (int part = 0; part < 2; ++part) {
         if (!nd[part]) continue;
-        // the first compiled configuration with 32 coefficients per thread covering these families
+        // the narrowest compiled configuration covering these families and
+        // lengths, with the most resident CTAs among those (the choice the
+        // autotuner makes on the benchmark batch; the serving loop's rule)
         const BatchConfig* cfgs = nullptr;
         const int ncfg = part ? batch_configs_i32(&cfgs) : batch_configs_i16(&cfgs);
+        int maxL = 0;
+        for (int i = 0; i < nd[part]; ++i) maxL = Ls[part][i] > maxL ? Ls[part][i] : maxL;
+        auto resident = [](const BatchConfig& c) { return c.occ ? c.occ : batch_min_blocks(c.i32, c.cta, c.elmax); };
         const BatchConfig* cfg = nullptr;
-        for (int c = 0; c < ncfg && !cfg; ++c)
-            if (cfgs[c].elmax == 5 && cfgs[c].cta == BATCH_CTA && (cfgs[c].set & fam_mask[part]) == fam_mask[part]) cfg = &cfgs[c];
+        for (int c = 0; c < ncfg; ++c)
+            if (cfgs[c].cta == BATCH_CTA && (cfgs[c].set & fam_mask[part]) == fam_mask[part] &&
+                config_fits(cfgs[c], maxL) &&
+                (!cfg || cfgs[c].elmax < cfg->elmax ||
+                 (cfgs[c].elmax == cfg->elmax && resident(cfgs[c]) > resident(*cfg))))
+                cfg = &cfgs[c];
         if (!cfg) return fail(GBNTT_ERR_ARG, "no persistent kernel covers these designs");
         // tiles, largest n first
         int order[GBNTT_NOALLOC_MAX_SEGMENTS];
