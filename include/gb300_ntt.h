@@ -159,8 +159,12 @@ typedef struct gbntt_batch gbntt_batch;
 
 /* flags: GBNTT_BATCH_NO_TUNE skips the autotuner, which otherwise times every
  * persistent-kernel configuration (coefficients per thread, hence threads
- * and CTAs per transform and polynomials per tile) on the batch itself at
- * creation and keeps the fastest.  Creation then writes the segments' outputs. */
+ * and CTAs per transform and polynomials per tile, and resident CTAs per SM)
+ * on the batch itself at creation and keeps the fastest.  A batch whose
+ * inputs and outputs fit in L2 is timed from HBM: creation then briefly
+ * allocates twice the L2 size of scratch to evict it between the timed
+ * launches (without room for it, the launches are timed back to back).
+ * Creation then writes the segments' outputs. */
 #define GBNTT_BATCH_NO_TUNE 0x1u
 int gbntt_batch_create(gbntt_batch** batch, const gbntt_segment* segs, uint32_t nsegs, uint32_t flags);
 int gbntt_batch_execute(gbntt_batch* batch, void* stream);
