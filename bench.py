@@ -81,6 +81,14 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
+def host_threads():
+    """The host cores this process may run on (the cgroup / affinity set, not the machine's count)."""
+    try:
+        return len(os.sched_getaffinity(0)) or 1
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
 def load_traffic():
     try:
         with open(os.path.join(HERE, "profiles", "traffic.json")) as f:
@@ -164,7 +172,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
+    threads = host_threads()
     inputs = make_inputs()
     from oracle import oracle
     plans = [oracle.Plan(oracle.R4_I16_FWD, n, q, root_of(q, n, g)) for (q, n, _, g) in SEGMENTS]
@@ -235,7 +243,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     batch.status()
     for i, (q, n, _, g) in enumerate(SEGMENTS):
-        want = oracle.Plan(oracle.R4_I16_FWD, n, q, root_of(q, n, g))(inputs[i], threads=os.cpu_count() or 1)
+        want = oracle.Plan(oracle.R4_I16_FWD, n, q, root_of(q, n, g))(inputs[i], threads=host_threads())
         assert np.array_equal(d_out[i].cpu().numpy(), want), "GPU output differs from the oracle"
 
     def timed(run, steps):
@@ -330,7 +338,7 @@ def run_ours(args):
         if dist:
             dist.destroy_process_group()
         return
-    threads = os.cpu_count() or 1
+    threads = host_threads()
     cpu = None
     if not args.skip_cpu:
         v, done, el = cpu_baseline(inputs, args.cpu_seconds, threads)
