@@ -315,6 +315,7 @@ int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t
     a.fneg = hp.r4_fneg;
     a.wc = hp.r4_wc;
     a.canonical = (flags & FLAG_CANONICAL) ? 1 : 0;
+    a.canon_c = hp.q >= 3 ? (int)((((uint64_t)1 << 32) + hp.q / 2) / hp.q) : 0;
     const bool inverse = (kind == K_R2_I16_INV || kind == K_R2_I32_INV || kind == K_R4_I16_INV);
     a.natural_in = ((flags & FLAG_NATURAL_ORDER) && inverse) ? 1 : 0;
     a.natural_out = ((flags & FLAG_NATURAL_ORDER) && !inverse) ? 1 : 0;

@@ -38,6 +38,7 @@ struct KArgs {
     int c;                // Barrett constant of the reduction (K = 16 or 32)
     int fneg, wc;         // radix-4 omega_4 and its multiplier
     int canonical;        // reduce outputs to [0, q)
+    int canon_c;          // its Barrett constant round(2^32 / q)
     int natural_in;       // input in natural order (inverse designs): bit reversal fused into the load
     int natural_out;      // output in natural order (forward designs): bit reversal fused into the store
     int scale;            // inverse designs: full Barrett multiplication by n^-1 fused into the store
@@ -143,10 +144,14 @@ __device__ __forceinline__ int fb16(int x, int fs, int wq, int q) {
     return wrap16(lo - sign * q);             // (:261-272)
 }
 
-// x mod q in [0, q)
-__device__ __forceinline__ int canon(int x, int q) {
-    int r = x % q;
-    return r < 0 ? r + q : r;
+// x mod q in [0, q) for any int32 x: one 32-bit Barrett step with
+// c = round(2^32 / q) leaves |r| <= 0.75 q (quotient error at most
+// 2^31 * 0.5 / 2^32 from c plus 0.5 from the rounding), and one conditional
+// addition of q finishes it; an integer division by a runtime q costs several
+// times as many instructions
+__device__ __forceinline__ int canon(int x, int q, int c) {
+    const int r = br32(x, c, q);
+    return r + ((r >> 31) & q);
 }
 
 // Which output options a design accepts (checked by the host as well): the
@@ -174,9 +179,9 @@ __device__ __forceinline__ void epilogue_all(int (&v)[E], const KArgs& a) {
         }
     }
     if (a.canonical) {
-        const int q = a.q;
+        const int q = a.q, c = a.canon_c;
 #pragma unroll
-        for (int k = 0; k < E; ++k) v[k] = canon(v[k], q);
+        for (int k = 0; k < E; ++k) v[k] = canon(v[k], q, c);
     }
 }
 

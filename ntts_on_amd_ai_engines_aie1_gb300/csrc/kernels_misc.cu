@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(256) k_r8_stage(const KArgs a, int L) {
         for (int k = 0; k < 8; ++k) {
             const int2 t = __ldg(&a.tab[k * M + i]);
             int z = r8red(y[k], t.x, t.y, a.q);
-            if (a.canonical) z = canon(z, a.q);
+            if (a.canonical) z = canon(z, a.q, a.canon_c);
             o[brev_c<3>(k)] = z;
         }
         int4 w;
