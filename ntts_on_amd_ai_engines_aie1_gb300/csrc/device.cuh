@@ -88,7 +88,7 @@ __device__ __forceinline__ KC make_kc(const KArgs& a) {
 __device__ __forceinline__ int rsz16(int p) { return (p + 0x7FFF + (int)((unsigned)p >> 31)) >> 16; }
 
 // round(p / 2^32), ties toward zero
-__device__ __forceinline__ int rsz32(long long p) {
+__host__ __device__ __forceinline__ int rsz32(long long p) {
     return (int)((p + 0x7FFFFFFFLL + (long long)((unsigned long long)p >> 63)) >> 32);
 }
 
@@ -118,7 +118,7 @@ __device__ __forceinline__ unsigned bm16_lo(int a, int t, int q) {
 }
 
 // int32 variants, computed modulo 2^32 like the int32 lanes
-__device__ __forceinline__ int br32(int a, int c, int q) {
+__host__ __device__ __forceinline__ int br32(int a, int c, int q) {
     return (int)((unsigned)a - (unsigned)rsz32((long long)a * c) * (unsigned)q);
 }
 __device__ __forceinline__ int bm32(int a, int tw, int wq, int q) {
@@ -149,7 +149,7 @@ __device__ __forceinline__ int fb16(int x, int fs, int wq, int q) {
 // 2^31 * 0.5 / 2^32 from c plus 0.5 from the rounding), and one conditional
 // addition of q finishes it; an integer division by a runtime q costs several
 // times as many instructions
-__device__ __forceinline__ int canon(int x, int q, int c) {
+__host__ __device__ __forceinline__ int canon(int x, int q, int c) {
     const int r = br32(x, c, q);
     return r + ((r >> 31) & q);
 }
