@@ -51,14 +51,16 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
     const int tid = threadIdx.x;
     const long long total = b.total_tiles;
 
-    auto seg_of = [&](long long t) {
-        int s = 0;
+    // segment of tile t, searched from segment `from`: a CTA's tiles come from
+    // the counter in increasing order, so its search never goes back
+    auto seg_of = [&](long long t, int from) {
+        int s = from < 0 ? 0 : from;
         while (s + 1 < b.nsegs && __ldg(&b.segs[s + 1].tile0) <= t) ++s;
         return s;
     };
     // thread 0: start the bulk load of tile t into buffer i
-    auto issue = [&](long long t, int i) {
-        const SegDev* sd = &b.segs[seg_of(t)];
+    auto issue = [&](long long t, int i, int from) {
+        const SegDev* sd = &b.segs[seg_of(t, from)];
         const long long lt = t - sd->tile0;
         const long long P = sd->polys_per_tile;
         const long long count = sd->a.batch;
@@ -79,7 +81,7 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
         sh_pending[1] = 0;
         sh_failed = 0;
         if (t0 < total) {
-            issue(t0, 0);
+            issue(t0, 0, 0);
             sh_pending[0] = 1;
         }
     }
@@ -90,14 +92,14 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
     int cur_seg = -1;
     KC kc;
     while (t < total) {
-        const int s = seg_of(t);
+        const int s = seg_of(t, cur_seg);
         const SegDev* sd = &b.segs[s];
         if (tid == 0) {
             const long long tn = (long long)atomicAdd(&b.ctr[CTR_NEXT], 1ull);
             sh_next = tn;
             if (tn < total) {
                 bulk_wait_read();           // the other buffer's last store has left shared memory
-                issue(tn, buf ^ 1);
+                issue(tn, buf ^ 1, s);
                 sh_pending[buf ^ 1] = 1;
             }
         }
@@ -176,8 +178,10 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
     __shared__ long long sh_next;
     const int tid = threadIdx.x;
     const long long total = b.total_tiles;
-    auto seg_of = [&](long long t) {
-        int s = 0;
+    // segment of tile t, searched from segment `from`: a CTA's tiles come from
+    // the counter in increasing order, so its search never goes back
+    auto seg_of = [&](long long t, int from) {
+        int s = from < 0 ? 0 : from;
         while (s + 1 < b.nsegs && __ldg(&b.segs[s + 1].tile0) <= t) ++s;
         return s;
     };
@@ -187,7 +191,7 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
     int cur_seg = -1;
     KC kc;
     while (t < total) {
-        const int s = seg_of(t);
+        const int s = seg_of(t, cur_seg);
         const SegDev* sd = &b.segs[s];
         if (s != cur_seg) {
             const int* src = reinterpret_cast<const int*>(&sd->a);
