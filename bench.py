@@ -599,6 +599,15 @@ PROFILE_CASES = {
     "r2f32_1m": (4, 1 << 20, 998244353, 565042129, 64),
     "r2g32_1m": (5, 1 << 20, 998244353, 565042129, 64),
     "r2f32_16k": (4, 1 << 14, 998244353, 666702199, 4096),
+    # canonical families (GBNTT_FLAG_CANONICAL)
+    "c_r4_1024": (2, 1024, 12289, 11580, 65536, 1),
+    "c_r2f16_1024": (0, 1024, 12289, 11580, 65536, 1),
+    "c_r2i16_1024": (1, 1024, 12289, 11580, 65536, 1),
+    "c_r2f32_4096": (4, 4096, 998244353, 63912897, 16384, 1),
+    "c_r2g32_4096": (5, 4096, 998244353, 63912897, 16384, 1),
+    "c_r2f32_16k": (4, 1 << 14, 998244353, 666702199, 4096, 1),
+    "c_r2g32_16k": (5, 1 << 14, 998244353, 666702199, 4096, 1),
+    "c_r2f32_32k": (4, 1 << 15, 998244353, pow(3, (998244353 - 1) >> 15, 998244353), 2048, 1),
     "batch_r4": None,   # the benchmark batch, 4x larger, persistent kernel
 }
 
@@ -638,8 +647,8 @@ def run_profile_case(name, launches=3):
     import ntts_on_amd_ai_engines_aie1_gb300 as gb
     if name == "batch_r4":
         return run_profile_batch(4, launches)
-    kind, n, q, root, polys = PROFILE_CASES[name]
-    plan = gb.Plan(kind, n, q, root)
+    kind, n, q, root, polys, *fl = PROFILE_CASES[name]
+    plan = gb.Plan(kind, n, q, root, 0, fl[0] if fl else 0)
     dt = torch.int32 if plan.elem_bytes == 4 else torch.int16
     g = torch.Generator(device="cuda").manual_seed(SEED)
     x = torch.randint(0, q, (polys, n), dtype=torch.int64, device="cuda", generator=g).to(dt)

@@ -74,7 +74,23 @@ typedef enum gbntt_status {
     GBNTT_ERR_ADMISSION = 10  /* a request could not be admitted (not enough free memory)       */
 } gbntt_status;
 
-/* Plan flags */
+/* Plan flags
+ *
+ * GBNTT_FLAG_CANONICAL: outputs are residues in [0, q) of the exact transform
+ * of the inputs (each input coefficient taken modulo q as a signed integer):
+ * the forward DFT in bit-reversed order, the inverse (BO in, NO out) without
+ * n^-1.  Those are the reference's outputs reduced modulo q wherever its
+ * int16/int32 lanes do not wrap; they run on a kernel family of their own
+ * (Shoup multiplication by precomputed quotients, lazily reduced 32-bit lanes,
+ * one reduction at the end; twiddle tables built on the device), for every
+ * transform design except the radix-8 single stage and the radix-8 chain with
+ * the reference's float multipliers, and int32 moduli below 2^30.
+ * GBNTT_FLAG_CANONICAL | GBNTT_FLAG_LANE_EXACT: the reference's own lane
+ * arithmetic (the default partial kernels, wraps included) reduced to [0, q),
+ * i.e. exactly the reference's residues also where its lanes wrap (full-range
+ * int16 input to the radix-2 inverse, the radix-4 designs at q > 16383, int32
+ * inverses at q >= 2^30); the designs the canonical family does not cover take
+ * this form whenever GBNTT_FLAG_CANONICAL is set. */
 #define GBNTT_FLAG_CANONICAL   0x1u  /* reduce outputs to [0, q)                                   */
 #define GBNTT_FLAG_R8_EXACT    0x2u  /* exact K=31 radix-8 multipliers (default for R8_I16_FWD)    */
 #define GBNTT_FLAG_R8_FLOAT    0x4u  /* the reference's float K=31 multipliers (src/twiddle.h:372;
@@ -82,7 +98,10 @@ typedef enum gbntt_status {
 #define GBNTT_FLAG_NATURAL_ORDER 0x8u /* bit-reversal unit fused into the transform: forward designs
                                         return natural order, inverse designs take natural order   */
 #define GBNTT_FLAG_SCALE_NINV 0x10u  /* int16 inverse designs: the full Barrett unit multiplying by
-                                        n^-1 (src/project.cpp:154) fused into the store            */
+                                        n^-1 (src/project.cpp:154) fused into the store (also the
+                                        canonical int32 inverse)                                    */
+#define GBNTT_FLAG_LANE_EXACT 0x20u  /* with GBNTT_FLAG_CANONICAL: the reference's lane arithmetic,
+                                        reduced to [0, q) (no effect without it)                   */
 
 typedef struct gbntt_plan gbntt_plan;
 
@@ -188,6 +207,17 @@ int gbntt_batch_set_io(gbntt_batch* batch, uint32_t seg, const void* d_in, void*
 /* Synchronous: GBNTT_ERR_TIMEOUT if a tile load of an earlier launch ran out
  * of its bounded wait (the error is cleared by the call). */
 int gbntt_batch_status(gbntt_batch* batch);
+/* Poll limit of the bounded wait for each tile load of the persistent kernel
+ * (batches, the no-alloc call, the serving loop), for launches enqueued after
+ * the call (a batch's CUDA graph keeps the limit it was captured with).  The
+ * default is GBNTT_WAIT_POLLS_DEFAULT; 0 makes every such wait give up at once.
+ * A tile whose wait runs out makes its CTA record GBNTT_ERR_TIMEOUT (reported
+ * by gbntt_batch_status, gbntt_noalloc_status and the server's waits), let its
+ * copies in flight land (those waits keep the default limit) and stop.  Small
+ * limits are for tests of that failure path.  No counterpart in the reference
+ * (AIE graphs have no runtime error channel). */
+#define GBNTT_WAIT_POLLS_DEFAULT 4194304u
+int gbntt_set_wait_limit(uint32_t polls);
 #define GBNTT_BQ_LAUNCHES 0   /* kernel launches per execute            */
 #define GBNTT_BQ_TILES    1   /* tiles of the persistent launches        */
 #define GBNTT_BQ_GRID     2   /* CTAs of the largest persistent launch   */
@@ -211,17 +241,24 @@ int gbntt_batch_destroy(gbntt_batch* batch);
  * cudaMalloc/cudaFree in the middle of a request) use this call instead.  It
  * runs the same persistent kernel on up to GBNTT_NOALLOC_MAX_SEGMENTS segments
  * (plans created beforehand, caller-owned device buffers), keeping descriptors
- * and counters in one fixed static device array (about 16 KB, held on every
+ * and counters in one fixed static device array (about 8 KB, held on every
  * GPU that loads the library until the process exits).  More segments are
- * rejected with GBNTT_ERR_ARG.  The first call on a device looks the array up
+ * rejected with GBNTT_ERR_ARG; every segment's configuration is checked before
+ * anything is enqueued.  The first call on a device looks the array up
  * (cudaGetSymbolAddress) with that device current; make that first call before
- * any stream capture.  Every call reuses the array and resets its counters, so
- * calls whose work overlaps on the GPU (different streams, no ordering
- * between them) race; serialise them on one stream.  No autotuning: the
- * narrowest compiled configuration covering the segments' designs and
- * lengths, with the most resident CTAs among those, is used. */
+ * any stream capture.  The descriptors reach the array through a one-CTA kernel
+ * whose launch parameters carry them (no copy from host memory).  Every call
+ * reuses the array and resets its tile counters, so calls whose work overlaps
+ * on the GPU (different streams, no ordering between them) race; serialise
+ * them on one stream.  No autotuning: the narrowest compiled configuration
+ * covering the segments' designs and lengths, with the most resident CTAs
+ * among those, is used. */
 #define GBNTT_NOALLOC_MAX_SEGMENTS 16
 int gbntt_batch_execute_noalloc(const gbntt_segment* segs, uint32_t nsegs, void* stream);
+/* Synchronous, on the current device: GBNTT_ERR_TIMEOUT if a tile load of an
+ * earlier gbntt_batch_execute_noalloc launch ran out of its bounded wait (its
+ * outputs are then incomplete); the call clears the error words it reports. */
+int gbntt_noalloc_status(void);
 
 /* ---- serving loop: continuous batching of transform requests ----
  * Requests (a plan of the server, host input, host output, polynomial count)

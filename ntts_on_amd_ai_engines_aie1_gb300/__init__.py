@@ -43,6 +43,7 @@ FLAG_R8_EXACT = 0x2
 FLAG_R8_FLOAT = 0x4
 FLAG_NATURAL_ORDER = 0x8     # bit reversal fused: forward returns / inverse takes natural order
 FLAG_SCALE_NINV = 0x10       # int16 inverse: full Barrett multiplication by n^-1 fused
+FLAG_LANE_EXACT = 0x20       # with FLAG_CANONICAL: the reference's lane arithmetic, then reduced
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported length", 3: "invalid modulus",
           4: "root of unity has the wrong order", 5: "radix-4 needs an even number of layers",
@@ -110,6 +111,9 @@ def lib():
         L.gbntt_server_submit_schedule.argtypes = [vp, u64, ctypes.POINTER(u32), ctypes.POINTER(vp),
                                                    ctypes.POINTER(vp), ctypes.POINTER(u64),
                                                    ctypes.POINTER(ctypes.c_double), ctypes.POINTER(u64)]
+        L.gbntt_batch_execute_noalloc.argtypes = [ctypes.POINTER(Segment), u32, vp]
+        L.gbntt_noalloc_status.argtypes = []
+        L.gbntt_set_wait_limit.argtypes = [u32]
         L.gbntt_launch_count.restype = u64
         L.gbntt_last_error.restype = ctypes.c_char_p
         L.gbntt_status_string.restype = ctypes.c_char_p
@@ -126,6 +130,23 @@ def _check(rc):
 def launch_count():
     """Kernels launched by the library so far in this process."""
     return int(lib().gbntt_launch_count())
+
+
+WAIT_POLLS_DEFAULT = 1 << 22
+
+
+def set_wait_limit(polls=WAIT_POLLS_DEFAULT):
+    """Poll limit of the persistent kernel's bounded tile-load waits for
+    launches enqueued from now on (default 2^22; 0: every wait gives up at
+    once).  Small limits make the waits run out on purpose, to test the
+    failure path."""
+    _check(lib().gbntt_set_wait_limit(int(polls)))
+
+
+def noalloc_status():
+    """Raises NTTError (GBNTT_ERR_TIMEOUT) if a launch of the no-allocation
+    batch entry point ran out of a bounded wait; clears the error."""
+    _check(lib().gbntt_noalloc_status())
 
 
 def host_tables(kind, n, q=0, root=0, factor=0, flags=0, which=0):

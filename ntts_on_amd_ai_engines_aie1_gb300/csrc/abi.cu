@@ -8,6 +8,7 @@
 #include <string>
 
 #include "../../include/gb300_ntt.h"
+#include "canon_tables.h"
 #include "device.cuh"
 #include "plan_internal.h"
 #include "tables.h"
@@ -64,6 +65,7 @@ int family_of(int kind) {
 }
 
 KernelInfo kernel_for(int fam, int L, bool br, bool lat) {
+    if (fam_canon(fam)) return kinfo_canon(fam, L, lat);
     switch (fam) {
     case F_R2F16: return kinfo_r2f16(L, lat);
     case F_R2I16: return kinfo_r2i16(L, lat);
@@ -235,8 +237,12 @@ int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t
         return fail(rc, err);
     }
     const HostPlan& hp = p->hp;
-    p->fam = family_of(kind);
-    p->br = (kind == K_R4_I16_INV);
+    // GBNTT_FLAG_CANONICAL without GBNTT_FLAG_LANE_EXACT: the canonical family
+    // of the design's direction and storage type (the two-pass int32 lengths
+    // keep the reference's lane arithmetic plus the final reduction)
+    const bool canon = canonical_fast(kind, hp.q, flags) && hp.L < 16;
+    p->fam = canon ? canonical_family(kind) : family_of(kind);
+    p->br = !canon && (kind == K_R4_I16_INV);
     if (p->fam >= 0 && hp.L >= 16) {
         p->large = large_info(p->fam, hp.L);
         if (!p->large.cols) {
@@ -282,8 +288,25 @@ int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t
     }
     // int16 radix-2/4 designs: (tw, w') packed into one word (both fit int16)
     const bool packed = (p->fam == F_R2F16 || p->fam == F_R2I16 || p->fam == F_R4F16);
+    const bool inverse = (kind == K_R2_I16_INV || kind == K_R2_I32_INV || kind == K_R4_I16_INV);
     std::vector<int32_t> dev_tab;
-    if (packed) {
+    if (canon) {
+        // canonical families: (w, w') pairs computed on the device
+        p->tab_bytes = canon_table_entries(hp.L, inverse) * sizeof(int2);
+        e = cudaMalloc(&p->d_tab, p->tab_bytes);
+        if (e != cudaSuccess) {
+            delete p;
+            return e == cudaErrorMemoryAllocation ? fail(GBNTT_ERR_NOMEM, "device allocation failed")
+                                                  : cuda_fail(e, "cudaMalloc");
+        }
+        e = make_canon_table(p->d_tab, hp.L, (uint32_t)hp.q, (uint32_t)hp.root, inverse, 0);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+        if (e != cudaSuccess) {
+            cudaFree(p->d_tab);
+            delete p;
+            return cuda_fail(e, "canonical table");
+        }
+    } else if (packed) {
         dev_tab.resize(hp.tab.size() / 2);
         for (size_t i = 0; i < dev_tab.size(); ++i)
             dev_tab[i] = (int32_t)(((uint32_t)hp.tab[2 * i] & 0xFFFFu) | ((uint32_t)hp.tab[2 * i + 1] << 16));
@@ -316,7 +339,19 @@ int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t
     a.wc = hp.r4_wc;
     a.canonical = (flags & FLAG_CANONICAL) ? 1 : 0;
     a.canon_c = hp.q >= 3 ? (int)((((uint64_t)1 << 32) + hp.q / 2) / hp.q) : 0;
-    const bool inverse = (kind == K_R2_I16_INV || kind == K_R2_I32_INV || kind == K_R4_I16_INV);
+    if (canon) {
+        a.canonical = 1;
+        a.cq = (unsigned)((((uint64_t)1) << 32) / (uint64_t)hp.q);
+        if (hp.elem_bytes == 2) {
+            const int64_t m = hp.q * ((32768 + hp.q - 1) / hp.q);     // a multiple of q, >= 2^15
+            a.in_off = (int)(2 * m);
+        } else {
+            a.in_off = (int)(hp.q - ((int64_t)1 << 31) % hp.q);      // residue of -2^31, in (0, q]
+        }
+        const uint64_t ninv = (uint64_t)modinv((int64_t)hp.n, hp.q);
+        a.ninv = (unsigned)ninv;
+        a.ninv_q = (unsigned)((ninv << 32) / (uint64_t)hp.q);
+    }
     a.natural_in = ((flags & FLAG_NATURAL_ORDER) && inverse) ? 1 : 0;
     a.natural_out = ((flags & FLAG_NATURAL_ORDER) && !inverse) ? 1 : 0;
     a.scale = (flags & FLAG_SCALE_NINV) ? 1 : 0;

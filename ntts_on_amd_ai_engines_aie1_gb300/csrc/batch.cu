@@ -3,7 +3,9 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <atomic>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -39,14 +41,35 @@ struct gbntt_batch {
         std::vector<int> user_index;    // caller's segment of each SegDev
         Layout zlay;                    // zero-copy launch (k_batch_zc), when a configuration has one
     };
-    Part parts[2];
+    Part parts[BATCH_PARTS];            // one persistent launch per storage type and arithmetic
     int nparts = 0;
     std::vector<int> part_of;           // segment -> part (or -1: separate per-plan launch)
     std::vector<int> index_in_part;
     std::vector<gbntt_segment> user;    // the caller's segments
     unsigned long long* d_ctr = nullptr;   // CTR_WORDS per part; then CTR_WORDS per part for zero copy
+                                           // (BATCH_PARTS each)
     cudaGraphExec_t graph = nullptr;
 };
+
+namespace gbntt {
+
+namespace {
+std::atomic<unsigned> g_wait_polls{BATCH_WAIT_POLLS};
+}
+
+unsigned batch_wait_polls() { return g_wait_polls.load(std::memory_order_relaxed); }
+
+cudaError_t raise_smem_limit(const void* fn, int bytes) {
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    cudaFuncAttributes at;
+    cudaError_t e = cudaFuncGetAttributes(&at, fn);
+    if (e != cudaSuccess) return e;
+    if (at.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+}  // namespace gbntt
 
 namespace {
 
@@ -59,6 +82,7 @@ int launch_layout(gbntt_batch* b, int pi, const gbntt_batch::Layout& lay, cudaSt
     bd.nsegs = (int)lay.segs.size();
     bd.total_tiles = lay.total_tiles;
     bd.ctr = b->d_ctr + CTR_WORDS * pi;
+    bd.wait_polls = batch_wait_polls();
     int sb = lay.stage_bytes;
     void* args[] = {&bd, &sb};
     cudaError_t e = cudaLaunchKernel(lay.cfg.fn, dim3(lay.grid), dim3(lay.cfg.cta), args, lay.smem, s);
@@ -215,7 +239,7 @@ int gbntt_internal_zc_plan(void** state, const gbntt_plan* p, const void* m_in, 
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaError_t e = cudaFuncSetAttribute(cfg->zfn, cudaFuncAttributeMaxDynamicSharedMemorySize, st.smem);
+        cudaError_t e = raise_smem_limit(cfg->zfn, st.smem);
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cfg->zfn, cfg->cta, st.smem);
         if (e != cudaSuccess || per_sm < 1)
             return batch_fail(GBNTT_ERR_CUDA, std::string("zero-copy kernel configuration: ") + cudaGetErrorString(e));
@@ -252,6 +276,7 @@ int gbntt_internal_zc_plan(void** state, const gbntt_plan* p, const void* m_in, 
     bd.nsegs = 1;
     bd.total_tiles = sd.tiles;
     bd.ctr = st.d_ctr;
+    bd.wait_polls = BATCH_WAIT_POLLS;   // the zero-copy kernel has no bounded waits
     int sb = st.stage;
     void* args[] = {&bd, &sb};
     const unsigned grid = (unsigned)std::min<long long>(st.grid_cap, sd.tiles);
@@ -274,6 +299,12 @@ void gbntt_internal_zc_free(void* state) {
 
 extern "C" {
 
+int gbntt_set_wait_limit(uint32_t polls) {
+    static_assert(GBNTT_WAIT_POLLS_DEFAULT == BATCH_WAIT_POLLS, "one default poll limit");
+    g_wait_polls.store(polls, std::memory_order_relaxed);
+    return GBNTT_OK;
+}
+
 int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t nsegs, uint32_t flags) {
     if (!out || (!segs && nsegs)) return batch_fail(GBNTT_ERR_ARG, "null argument");
     *out = nullptr;
@@ -287,7 +318,7 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
         return gbntt_internal_plan_L(segs[x].plan) > gbntt_internal_plan_L(segs[y].plan);
     });
-    int pid[2] = {-1, -1};
+    int pid[BATCH_PARTS] = {-1, -1, -1, -1};
     for (int k : order) {
         const gbntt_segment& u = segs[k];
         if (!u.plan) { delete b; return batch_fail(GBNTT_ERR_ARG, "segment without a plan"); }
@@ -301,7 +332,7 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
         gbntt_internal_plan_args(u.plan, &fam, &L, &eb, &a);
         if (fam < 0 || !variant_supported(fam, L) || u.d_in == u.d_out || u.count == 0) continue;   // per-plan launch
         const bool i32 = fam_i32(fam);
-        int& id = pid[i32 ? 1 : 0];
+        int& id = pid[batch_part_of(fam)];
         if (id < 0) {
             id = b->nparts++;
             b->parts[id].i32 = i32;
@@ -330,6 +361,10 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
                 lay.cfg = cfgs[c];
                 part.layouts.push_back(lay);
             }
+        if (part.layouts.empty()) {
+            gbntt_batch_destroy(b);
+            return batch_fail(GBNTT_ERR_ARG, "no persistent kernel covers these designs");
+        }
         if (flags & GBNTT_BATCH_NO_TUNE) part.layouts.resize(1);   // the first (widest, most specific) one
         // zero copy: the narrowest covering configuration
         for (int c = 0; c < ncfg; ++c)
@@ -381,7 +416,7 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
             lay.stage_bytes = (lay.stage_bytes + 127) & ~127;
             lay.smem = SMEM_HEADER + (zc ? 1 : 2) * lay.stage_bytes + lay.smem;
             const void* fn = zc ? lay.cfg.zfn : lay.cfg.fn;
-            cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, lay.smem);
+            cudaError_t e = raise_smem_limit(fn, lay.smem);
             int per_sm = 0;
             if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, lay.cfg.cta, lay.smem);
             if (e != cudaSuccess || per_sm < 1) {
@@ -403,8 +438,8 @@ int gbntt_batch_create(gbntt_batch** out, const gbntt_segment* segs, uint32_t ns
             }
         }
     }
-    cudaError_t e = cudaMalloc(&b->d_ctr, sizeof(unsigned long long) * CTR_WORDS * 4);
-    if (e == cudaSuccess) e = cudaMemset(b->d_ctr, 0, sizeof(unsigned long long) * CTR_WORDS * 4);
+    cudaError_t e = cudaMalloc(&b->d_ctr, sizeof(unsigned long long) * CTR_WORDS * 2 * BATCH_PARTS);
+    if (e == cudaSuccess) e = cudaMemset(b->d_ctr, 0, sizeof(unsigned long long) * CTR_WORDS * 2 * BATCH_PARTS);
     if (e != cudaSuccess) {
         gbntt_batch_destroy(b);
         return batch_fail(GBNTT_ERR_NOMEM, "batch scratch allocation failed");
@@ -508,7 +543,8 @@ int gbntt_batch_execute_host(gbntt_batch* b, const void* const* h_in, void* cons
             bd.segs = lay.d_segs;
             bd.nsegs = (int)lay.segs.size();
             bd.total_tiles = lay.total_tiles;
-            bd.ctr = b->d_ctr + CTR_WORDS * (2 + i);
+            bd.ctr = b->d_ctr + CTR_WORDS * (BATCH_PARTS + i);
+            bd.wait_polls = BATCH_WAIT_POLLS;
             int sb = lay.stage_bytes;
             void* args[] = {&bd, &sb};
             e = cudaLaunchKernel(lay.cfg.zfn, dim3(lay.grid), dim3(lay.cfg.cta), args, lay.smem, s);
@@ -577,10 +613,12 @@ int gbntt_batch_set_io(gbntt_batch* b, uint32_t seg, const void* d_in, void* d_o
 
 int gbntt_batch_status(gbntt_batch* b) {
     if (!b) return batch_fail(GBNTT_ERR_ARG, "batch is null");
-    unsigned long long w[CTR_WORDS * 2];
+    unsigned long long w[CTR_WORDS * BATCH_PARTS];
     cudaError_t e = cudaMemcpy(w, b->d_ctr, sizeof(w), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return batch_fail(GBNTT_ERR_CUDA, std::string("status read: ") + cudaGetErrorString(e));
-    if (w[CTR_ERROR] || w[CTR_WORDS + CTR_ERROR]) {
+    bool timed_out = false;
+    for (int i = 0; i < BATCH_PARTS; ++i) timed_out |= w[CTR_WORDS * i + CTR_ERROR] != 0;
+    if (timed_out) {
         cudaMemset(b->d_ctr, 0, sizeof(w));
         return batch_fail(GBNTT_ERR_TIMEOUT, "a tile load did not arrive within the wait limit");
     }

@@ -11,12 +11,15 @@ const void* batch_kernels_i16_w32(int el, int set, int occ);
 const void* batch_kernels_i16_w32g(int el, int set, int occ);
 const void* batch_kernels_i16_w16(int el, int set, int occ);
 const void* batch_kernels_i16_w16g(int el, int set, int occ);
+const void* batch_kernels_c16(int el, int set, int occ);
+const void* batch_zc_kernel_c16(int set, int el);
 
 namespace {
 constexpr int R2 = (1 << F_R2F16) | (1 << F_R2I16);
 constexpr int R4 = 1 << F_R4F16;
 constexpr int R8 = 1 << F_R8F16;
 constexpr int ALL16 = R2 | R4 | R8;
+constexpr int C16 = (1 << F_C16F) | (1 << F_C16I);   // canonical forward + inverse
 
 struct Key {
     int el, set, occ;
@@ -29,6 +32,9 @@ struct Key {
 constexpr Key kKeys[] = {
     {6, R4, 0}, {5, R4, 0}, {6, R2, 0}, {5, R2, 0}, {6, R8, 0}, {5, R8, 0}, {5, ALL16, 0},
     {4, R4, 0}, {4, R4, 5}, {4, R4, 6}, {4, R2, 0}, {4, R2, 5}, {4, R8, 0}, {4, R8, 5}, {4, ALL16, 0},
+    // canonical families: 16 coefficients per thread at 4, 5 and 6 CTAs/SM, 32 at 3
+    // (8 per thread at 8 CTAs/SM spilled at its 32-register budget)
+    {4, C16, 6}, {4, C16, 5}, {4, C16, 0}, {5, C16, 0},
 };
 constexpr int kN = (int)(sizeof(kKeys) / sizeof(kKeys[0]));
 BatchConfig kI16[kN];
@@ -40,9 +46,11 @@ int batch_configs_i16(const BatchConfig** out) {
             const Key k = kKeys[i];
             const void* fn = nullptr;
             for (auto get : {batch_kernels_i16_w64, batch_kernels_i16_w32, batch_kernels_i16_w32g,
-                             batch_kernels_i16_w16, batch_kernels_i16_w16g})
+                             batch_kernels_i16_w16, batch_kernels_i16_w16g, batch_kernels_c16})
                 if (!fn) fn = get(k.el, k.set, k.occ);
-            kI16[i] = BatchConfig{false, k.el, k.set, fn, batch_zc_kernel_i16(k.set, k.el), BATCH_CTA, k.occ};
+            const void* zfn = k.set == C16 ? (k.occ == 0 ? batch_zc_kernel_c16(k.set, k.el) : nullptr)
+                                           : batch_zc_kernel_i16(k.set, k.el);
+            kI16[i] = BatchConfig{false, k.el, k.set, fn, zfn, BATCH_CTA, k.occ};
         }
         return true;
     }();

@@ -6,10 +6,12 @@
 namespace gbntt {
 
 const void* batch_kernels_i32_w16(int occ, bool zero_copy);
+const void* batch_kernels_c32(int el, int occ, bool zero_copy);
 
 namespace {
 constexpr int I32SET = (1 << F_R2F32) | (1 << F_R2G32);
-BatchConfig kI32[3];
+constexpr int C32 = (1 << F_C32F) | (1 << F_C32I);   // canonical forward + inverse
+BatchConfig kI32[6];
 }  // namespace
 
 int batch_configs_i32(const BatchConfig** out) {
@@ -19,11 +21,16 @@ int batch_configs_i32(const BatchConfig** out) {
         kI32[1] = BatchConfig{true, 4, I32SET, batch_kernels_i32_w16(0, false), batch_kernels_i32_w16(0, true),
                               BATCH_CTA, 0};
         kI32[2] = BatchConfig{true, 4, I32SET, batch_kernels_i32_w16(4, false), nullptr, BATCH_CTA, 4};
+        kI32[3] = BatchConfig{true, 5, C32, batch_kernels_c32(5, 0, false), batch_kernels_c32(5, 0, true),
+                              BATCH_CTA, 0};
+        kI32[4] = BatchConfig{true, 4, C32, batch_kernels_c32(4, 0, false), batch_kernels_c32(4, 0, true),
+                              BATCH_CTA, 0};
+        kI32[5] = BatchConfig{true, 4, C32, batch_kernels_c32(4, 4, false), nullptr, BATCH_CTA, 4};
         return true;
     }();
     (void)built;
     *out = kI32;
-    return 3;
+    return 6;
 }
 
 }  // namespace gbntt

@@ -24,6 +24,20 @@ constexpr int BATCH_CTA = 256;
     X(F_R2G32, 2) X(F_R2G32, 3) X(F_R2G32, 4) X(F_R2G32, 5) X(F_R2G32, 6) X(F_R2G32, 7) X(F_R2G32, 8)         \
     X(F_R2G32, 9) X(F_R2G32, 10) X(F_R2G32, 11) X(F_R2G32, 12) X(F_R2G32, 13)
 
+// the canonical families (int16 storage 2^3 .. 2^12, int32 2^2 .. 2^13: every
+// polynomial is a multiple of 16 bytes, as the bulk copies require)
+#define GB_C16_VARIANTS(X)                                                                                   \
+    X(F_C16F, 3) X(F_C16F, 4) X(F_C16F, 5) X(F_C16F, 6) X(F_C16F, 7) X(F_C16F, 8) X(F_C16F, 9)               \
+    X(F_C16F, 10) X(F_C16F, 11) X(F_C16F, 12)                                                                \
+    X(F_C16I, 3) X(F_C16I, 4) X(F_C16I, 5) X(F_C16I, 6) X(F_C16I, 7) X(F_C16I, 8) X(F_C16I, 9)               \
+    X(F_C16I, 10) X(F_C16I, 11) X(F_C16I, 12)
+#define GB_C32_VARIANTS(X)                                                                                   \
+    X(F_C32F, 2) X(F_C32F, 3) X(F_C32F, 4) X(F_C32F, 5) X(F_C32F, 6) X(F_C32F, 7) X(F_C32F, 8)               \
+    X(F_C32F, 9) X(F_C32F, 10) X(F_C32F, 11) X(F_C32F, 12) X(F_C32F, 13)                                     \
+    X(F_C32I, 2) X(F_C32I, 3) X(F_C32I, 4) X(F_C32I, 5) X(F_C32I, 6) X(F_C32I, 7) X(F_C32I, 8)               \
+    X(F_C32I, 9) X(F_C32I, 10) X(F_C32I, 11) X(F_C32I, 12) X(F_C32I, 13)
+#define GB_ALL_VARIANTS(X) GB_I16_VARIANTS(X) GB_I32_VARIANTS(X) GB_C16_VARIANTS(X) GB_C32_VARIANTS(X)
+
 // a polynomial of 2^L coefficients fits one CTA of `cta` threads at 2^elmax per thread
 __host__ __device__ constexpr bool batch_fits(int L, int cta, int elmax) {
     return (1 << (L - (L < elmax ? L : elmax))) <= cta;
@@ -112,7 +126,7 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
             __syncthreads();
             kc = make_kc(*ka);
         }
-        if (!mbar_wait(&bar[buf], (phases >> buf) & 1u)) sh_failed = 1;
+        if (!mbar_wait(&bar[buf], (phases >> buf) & 1u, b.wait_polls)) sh_failed = 1;
         phases ^= 1u << buf;
         const long long lt = t - sd->tile0;
         const int P = sd->polys_per_tile;
@@ -125,8 +139,7 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
         if constexpr (fam_i32(F) == I32 && ((SET >> F) & 1) && batch_fits(L, CTA, ELMAX))            \
             tile_transform<F, L, CTA, ELMAX>(st, xbuf, kc, *ka, np);                                       \
         break;
-            GB_I16_VARIANTS(GB_CASE)
-            GB_I32_VARIANTS(GB_CASE)
+            GB_ALL_VARIANTS(GB_CASE)
 #undef GB_CASE
             default: break;
         }
@@ -146,10 +159,11 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
     if (tid == 0) {
         if (sh_failed) {
             atomicMax(&b.ctr[CTR_ERROR], (unsigned long long)BERR_TIMEOUT);
-            // let a prefetch that is still in flight land before the CTA leaves (bounded)
-            // (bar[buf]'s parity bit was already advanced past the load it waited for)
+            // let a prefetch that is still in flight land before the CTA leaves
+            // (bounded by the full limit whatever b.wait_polls is; bar[buf]'s
+            // parity bit was already advanced past the load it waited for)
             for (int i = 0; i < 2; ++i)
-                if (sh_pending[i]) mbar_wait(&bar[i], ((phases >> i) & 1u) ^ (i == buf ? 1u : 0u));
+                if (sh_pending[i]) mbar_wait(&bar[i], ((phases >> i) & 1u) ^ (i == buf ? 1u : 0u), BATCH_WAIT_POLLS);
         }
         bulk_wait_all();
         __threadfence();
@@ -217,8 +231,7 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
         if constexpr (fam_i32(F) == I32 && ((SET >> F) & 1) && batch_fits(L, CTA, ELMAX))            \
             tile_transform<F, L, CTA, ELMAX>(stage, xbuf, kc, *ka, np);                                    \
         break;
-            GB_I16_VARIANTS(GB_CASE)
-            GB_I32_VARIANTS(GB_CASE)
+            GB_ALL_VARIANTS(GB_CASE)
 #undef GB_CASE
             default: break;
         }
@@ -240,8 +253,7 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
 
 inline bool variant_supported(int fam, int L) {
 #define GB_HAS(F, L_) if (fam == F && L == L_) return true;
-    GB_I16_VARIANTS(GB_HAS)
-    GB_I32_VARIANTS(GB_HAS)
+    GB_ALL_VARIANTS(GB_HAS)
 #undef GB_HAS
     return false;
 }
@@ -260,6 +272,22 @@ struct BatchConfig {
 
 // the configuration carries a transform of 2^L coefficients
 inline bool config_fits(const BatchConfig& c, int L) { return batch_fits(L, c.cta, c.elmax); }
+
+// the persistent launch of a batch part: storage type and arithmetic
+// (the reference's lanes or the canonical families) -- 4 parts
+__host__ __device__ constexpr int batch_part_of(int fam) { return (fam_i32(fam) ? 1 : 0) | (fam_canon(fam) ? 2 : 0); }
+constexpr int BATCH_PARTS = 4;
+
+// Raises a kernel's dynamic shared-memory limit on the current device to at
+// least `bytes`, never lowering it: several batches, servers and no-alloc calls
+// share one kernel function with different needs, and a lower setting made
+// after a higher one would make the earlier user's launches fail.  Serialised
+// across host threads (batch.cu).
+cudaError_t raise_smem_limit(const void* fn, int bytes);
+
+// the poll limit of tile-load waits for launches enqueued now
+// (gbntt_set_wait_limit; BATCH_WAIT_POLLS by default)
+unsigned batch_wait_polls();
 
 // the configurations compiled into the library
 int batch_configs_i16(const BatchConfig** out);

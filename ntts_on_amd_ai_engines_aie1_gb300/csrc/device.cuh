@@ -15,6 +15,10 @@
 //     symmetric_zero mode (nearest, ties toward zero);
 //   * int16 / int32 two's-complement wrap wherever the AIE code stores to
 //     int16 / int32 lanes (saturation mode none).
+// The canonical families (F_C16F ... F_C32I) run the same transforms with
+// their own arithmetic instead: Shoup multiplication by precomputed quotients
+// and lazily reduced 32-bit lanes, reduced to [0, q) once at the end (see
+// "canonical arithmetic" below).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -23,7 +27,18 @@
 
 namespace gbntt {
 
-enum Fam { F_R2F16 = 0, F_R2I16 = 1, F_R4F16 = 2, F_R8F16 = 3, F_R2F32 = 4, F_R2G32 = 5, F_NUM = 6 };
+// F_R2F16 ... F_R2G32: the reference's lane arithmetic (partially reduced
+// outputs, bit for bit).  F_C16F ... F_C32I: canonical arithmetic, forward
+// (natural order in, bit-reversed out) and inverse (bit-reversed in, natural
+// out, no n^-1), int16 or int32 storage; every forward design of the reference
+// computes the forward transform's residues and every inverse design the
+// inverse's, so one canonical family per direction and storage type serves
+// them all.
+enum Fam {
+    F_R2F16 = 0, F_R2I16 = 1, F_R4F16 = 2, F_R8F16 = 3, F_R2F32 = 4, F_R2G32 = 5,
+    F_C16F = 6, F_C16I = 7, F_C32F = 8, F_C32I = 9, F_NUM = 10
+};
+__host__ __device__ constexpr bool fam_canon(int fam) { return fam >= F_C16F && fam <= F_C32I; }
 
 // Per-launch arguments (by value; the kernel reads the constants from the
 // parameter bank).
@@ -49,6 +64,11 @@ struct KArgs {
     int f8[64];           // radix-8 matrix [m][k]
     int f8s[4];           // f1, f2, f3
     int ftail[16];        // tail matrix [m][k]
+    // canonical families (tab: (w, floor(w 2^32 / q)) pairs)
+    unsigned cq;          // floor(2^32 / q)
+    int in_off;           // int16: 2M, M = q ceil(2^15 / q); int32: q - (2^31 mod q)
+    unsigned ninv, ninv_q;   // n^-1 mod q and its Shoup quotient (n^-1 scaling of inverse designs)
+    const int2* twist;    // four-step row twist factors (two-pass canonical int32 transforms)
 };
 
 // The scalar constants of one design, held in registers while a polynomial is
@@ -59,6 +79,7 @@ struct KC {
     const int* f8;
     const int* ftail;
     int q, c, fneg, wc, r8_sym, tail_wq, f1, f2, f3, wq1;
+    int in_off;
 };
 
 __device__ __forceinline__ KC make_kc(const KArgs& a) {
@@ -77,6 +98,7 @@ __device__ __forceinline__ KC make_kc(const KArgs& a) {
     k.f1 = a.f8s[1];
     k.f2 = a.f8s[2];
     k.f3 = a.f8s[3];
+    k.in_off = a.in_off;
     return k;
 }
 
@@ -154,21 +176,101 @@ __host__ __device__ __forceinline__ int canon(int x, int q, int c) {
     return r + ((r >> 31) & q);
 }
 
+// ---------------------------------------------------------------------------
+// canonical arithmetic (families F_C16F ... F_C32I)
+//
+// Lanes are unsigned 32-bit values congruent to the coefficient, reduced only
+// as far as the next operation needs:
+//   * Shoup multiplication (V. Shoup's precomputed-quotient modular multiply,
+//     as in D. Harvey, "Faster arithmetic for number-theoretic transforms",
+//     2014): for a twiddle w < q with w' = floor(w 2^32 / q) and any y < 2^32,
+//     y w - floor(y w' / 2^32) q lies in [0, 2q); the low 32 bits of the two
+//     products give it exactly (mul.hi + two IMADs);
+//   * a Cooley-Tukey butterfly x +- t (t the Shoup product) leaves x + t and
+//     x - t + 2q, so the bound on the lanes grows by 2q per layer.  int16
+//     moduli (q < 2^15) start below 2^18 and never come near 2^32 in 12
+//     layers: no correction at all.  int32 moduli (q < 2^30) keep the Harvey
+//     bound: x is brought from [0, 4q) to [0, 2q) before each butterfly
+//     (one subtraction and an unsigned minimum), outputs stay below 4q;
+//   * one reduction to [0, q) at the end.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned shoup_mul(unsigned y, unsigned w, unsigned wq, unsigned q) {
+    return y * w - __umulhi(y, wq) * q;
+}
+// [0, 2m) -> [0, m) for an unsigned lane (x - m wraps to a large value when x < m)
+__device__ __forceinline__ unsigned lazy_sub(unsigned x, unsigned m) { return min(x, x - m); }
+
+// int32 input coefficient (any signed value) -> a lane in [0, 2q): x + 2^31 is
+// reduced by one Barrett step with floor(2^32 / q) (error below 2q), then the
+// residue of -2^31 is added back and the sum folded below 2q
+__device__ __forceinline__ unsigned canon_in32(int x, unsigned q, unsigned cq, unsigned k31) {
+    const unsigned u = (unsigned)x ^ 0x80000000u;
+    const unsigned r = u - __umulhi(u, cq) * q;
+    return lazy_sub(r + k31, 2u * q);
+}
+// a lane below 2^32 -> [0, q)
+__device__ __forceinline__ unsigned canon_out(unsigned v, unsigned q, unsigned cq) {
+    return lazy_sub(v - __umulhi(v, cq) * q, q);
+}
+
 // Which output options a design accepts (checked by the host as well): the
 // fused n^-1 scaling belongs to the int16 inverse designs, natural-order input
 // to the inverse designs and natural-order output to the forward designs.
 // BR marks the radix-4 inverse, which runs the radix-4 kernel between two bit
 // reversals.  Gating them at compile time keeps their registers and code out
 // of the designs that never use them.
-__host__ __device__ constexpr bool fam_scales(int fam, bool br) { return fam == F_R2I16 || (fam == F_R4F16 && br); }
+__host__ __device__ constexpr bool fam_scales(int fam, bool br) {
+    return fam == F_R2I16 || (fam == F_R4F16 && br) || fam == F_C16I || fam == F_C32I;
+}
 __host__ __device__ constexpr bool fam_natural_in(int fam, bool br) {
-    return fam == F_R2I16 || fam == F_R2G32 || (fam == F_R4F16 && br);
+    return fam == F_R2I16 || fam == F_R2G32 || (fam == F_R4F16 && br) || fam == F_C16I || fam == F_C32I;
 }
 __host__ __device__ constexpr bool fam_natural_out(int fam, bool br) { return !fam_natural_in(fam, br); }
 
 // The output epilogue: fused n^-1 scaling (SCALE designs), canonical form.
 // The flags are read from the kernel arguments where they are used, so they
 // hold no registers through the transform.
+template <bool SCALE, int E>
+__device__ __forceinline__ void epilogue_all(int (&v)[E], const KArgs& a);
+
+// Canonical families: every lane to [0, q), or n^-1 times it (a Shoup
+// multiplication, [0, 2q), then one subtraction) for a scaled inverse.
+template <int E>
+__device__ __forceinline__ void epilogue_canon(int (&v)[E], const KArgs& a, bool scale) {
+    const unsigned q = (unsigned)a.q;
+    if (scale) {
+        const unsigned w = a.ninv, wq = a.ninv_q;
+#pragma unroll
+        for (int k = 0; k < E; ++k) v[k] = (int)lazy_sub(shoup_mul((unsigned)v[k], w, wq, q), q);
+    } else {
+        const unsigned cq = a.cq;
+#pragma unroll
+        for (int k = 0; k < E; ++k) v[k] = (int)canon_out((unsigned)v[k], q, cq);
+    }
+}
+
+// the epilogue of family FAM (BR: the radix-4 inverse's form)
+template <int FAM, bool BR, int E>
+__device__ __forceinline__ void epilogue(int (&v)[E], const KArgs& a) {
+    if constexpr (fam_canon(FAM)) {
+        epilogue_canon(v, a, fam_scales(FAM, BR) && a.scale);
+    } else {
+        epilogue_all<fam_scales(FAM, BR)>(v, a);
+    }
+}
+
+// The input prologue: canonical int32 lanes start in [0, 2q) (int16 inputs
+// stay raw; the first layer adds an offset instead).
+template <int FAM, int E>
+__device__ __forceinline__ void prologue(int (&v)[E], const KArgs& a) {
+    if constexpr (FAM == F_C32F || FAM == F_C32I) {
+        const unsigned q = (unsigned)a.q, cq = a.cq, k31 = (unsigned)a.in_off;
+#pragma unroll
+        for (int k = 0; k < E; ++k) v[k] = (int)canon_in32(v[k], q, cq, k31);
+    }
+}
+
 template <bool SCALE, int E>
 __device__ __forceinline__ void epilogue_all(int (&v)[E], const KArgs& a) {
     if constexpr (SCALE) {
@@ -189,9 +291,13 @@ __device__ __forceinline__ void epilogue_all(int (&v)[E], const KArgs& a) {
 // compile-time schedule
 // ---------------------------------------------------------------------------
 
-__host__ __device__ constexpr bool fam_i32(int fam) { return fam == F_R2F32 || fam == F_R2G32; }
+__host__ __device__ constexpr bool fam_i32(int fam) {
+    return fam == F_R2F32 || fam == F_R2G32 || fam == F_C32F || fam == F_C32I;
+}
 // forward designs consume position bits from the top, inverse ones from the bottom
-__host__ __device__ constexpr bool topdown(int fam) { return fam != F_R2I16 && fam != F_R2G32; }
+__host__ __device__ constexpr bool topdown(int fam) {
+    return fam != F_R2I16 && fam != F_R2G32 && fam != F_C16I && fam != F_C32I;
+}
 __host__ __device__ constexpr int nsteps(int fam, int L) {
     return fam == F_R4F16 ? L / 2 : fam == F_R8F16 ? L / 3 + (L % 3 ? 1 : 0) : L;
 }
@@ -471,7 +577,45 @@ __device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const
 #pragma unroll
     for (int r = 0; r < (E >> W); ++r) {
         const int k0 = ((r >> KB) << (KB + W)) | (r & ((1 << KB) - 1));
-        if constexpr (FAM == F_R2F16 || FAM == F_R2F32) {
+        if constexpr (fam_canon(FAM)) {
+            // canonical Cooley-Tukey butterfly (x, y) -> (x + w y, x - w y).
+            // Forward: layer S pairs the positions differing in bit B = L-1-S,
+            // w = root^bitrev_{L-1}(block), block = the position bits above B
+            // (one table of n/2 entries serves every layer).  Inverse on
+            // bit-reversed input: bit B = S, w = root^(-j 2^(L-1-B)) with
+            // j = the position bits below B, at table entry 2^B + j.
+            static_assert(!HIB && XC == 0, "the canonical families run whole sub-transforms");
+            const int k1 = k0 | (1 << KB);
+            const unsigned uq = (unsigned)q, q2 = uq << 1;
+            if constexpr (S == 0) {
+                // the first layer has the twiddle 1 everywhere (block 0 of
+                // the forward transform, span 1 of the inverse one)
+                if constexpr (fam_i32(FAM)) {
+                    // lanes in [0, 2q) from the prologue
+                    const unsigned x = (unsigned)v[k0], y = (unsigned)v[k1];
+                    v[k0] = (int)(x + y);
+                    v[k1] = (int)(x + q2 - y);
+                } else {
+                    // raw int16 inputs in [-2^15, 2^15): adding 2M (a multiple
+                    // of q, M >= 2^15) makes both lanes non-negative, below 2^18
+                    const int x = v[k0], y = v[k1];
+                    v[k0] = x + y + a.in_off;
+                    v[k1] = x - y + a.in_off;
+                }
+            } else {
+                int2 t;
+                if constexpr (topdown(FAM)) {
+                    t = __ldg(&a.tab[posmap<LO, EL>(g, k0) >> (B + 1)]);
+                } else {
+                    t = __ldg(&a.tab[(1 << B) + (posmap<LO, EL>(g, k0) & ((1 << B) - 1))]);
+                }
+                unsigned x = (unsigned)v[k0];
+                if constexpr (fam_i32(FAM)) x = lazy_sub(x, q2);
+                const unsigned m = shoup_mul((unsigned)v[k1], (unsigned)t.x, (unsigned)t.y, uq);
+                v[k0] = (int)(x + m);
+                v[k1] = (int)(x + q2 - m);
+            }
+        } else if constexpr (FAM == F_R2F16 || FAM == F_R2F32) {
             // forward CT layer S: block = position bits above B (src/kernels/
             // ntt_r2_kernels.cc:434-472, ntt_r2_int32_kernels.cc:267-295)
             const int k1 = k0 | (1 << KB);
@@ -768,9 +912,10 @@ __device__ __forceinline__ void k_ntt_body(const KArgs& a) {
     } else if constexpr (fam_natural_in(FAM, BR)) {
         if (a.natural_in) permute_br<L, EL, LO0>(v, sp, g);
     }
+    prologue<FAM>(v, a);
     const KC kc = make_kc(a);
     run_steps<FAM, L, EL>(v, sp, g, kc, std::make_integer_sequence<int, NS>{});
-    epilogue_all<fam_scales(FAM, BR)>(v, a);
+    epilogue<FAM, BR>(v, a);
     if constexpr (BR) {
         permute_br<L, EL, LOZ>(v, sp, g);
     } else if constexpr (fam_natural_out(FAM, BR)) {
@@ -784,7 +929,7 @@ __device__ __forceinline__ void k_ntt_body(const KArgs& a) {
 // throughput by up to a fifth on GB300; the same hint made the radix-2 and
 // radix-8 int16 code a fifth slower, so those keep the compiler's default.
 __host__ __device__ constexpr bool kntt_two_ctas(int fam, int threads) {
-    return threads <= 256 && (fam_i32(fam) || fam == F_R4F16);
+    return threads <= 256 && !fam_canon(fam) && (fam_i32(fam) || fam == F_R4F16);
 }
 
 template <int FAM, int L, int EL, int P, bool BR>
@@ -862,6 +1007,8 @@ KernelInfo kinfo_r2f32(int L, bool lat);
 KernelInfo kinfo_r2g32(int L, bool lat);
 KernelInfo kinfo_r4(int L, bool br, bool lat);
 KernelInfo kinfo_r8(int L, bool lat);
+// canonical families (kernels_c16.cu, kernels_c32.cu)
+KernelInfo kinfo_canon(int fam, int L, bool lat);
 
 // two-pass schedule for int32 transforms longer than one CTA holds (kernels_large.cu)
 struct LargeInfo {

@@ -1,5 +1,5 @@
 // noalloc.cu -- gbntt_batch_execute_noalloc: the persistent batch kernel run
-// without any device allocation.
+// without any device allocation, and gbntt_noalloc_status.
 //
 // gbntt_batch_create allocates device memory for the tile descriptors and the
 // tile counters of a batch.  Some callers cannot allocate device memory at the
@@ -25,12 +25,30 @@ using namespace gbntt;
 namespace {
 
 // descriptors of up to GBNTT_NOALLOC_MAX_SEGMENTS segments, then the tile
-// counters of the (at most two) persistent launches
+// counters of the (at most BATCH_PARTS) persistent launches
 constexpr size_t NOALLOC_DESC_BYTES = sizeof(SegDev) * GBNTT_NOALLOC_MAX_SEGMENTS;
 constexpr size_t NOALLOC_CTR_OFFSET = (NOALLOC_DESC_BYTES + 255) & ~size_t(255);
-constexpr size_t NOALLOC_SCRATCH_BYTES = NOALLOC_CTR_OFFSET + 2 * CTR_WORDS * sizeof(unsigned long long);
+constexpr size_t NOALLOC_CTR_BYTES = BATCH_PARTS * CTR_WORDS * sizeof(unsigned long long);
+constexpr size_t NOALLOC_SCRATCH_BYTES = NOALLOC_CTR_OFFSET + NOALLOC_CTR_BYTES;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+// The descriptors travel as a kernel parameter (copied by the launch itself)
+// and a one-CTA kernel writes them into the array: no host staging buffer, no
+// copy from pageable memory.
+struct DescBlock {
+    SegDev d[GBNTT_NOALLOC_MAX_SEGMENTS];
+    int count;
+};
+static_assert(sizeof(DescBlock) < 30000, "the descriptor block must fit the kernel parameter space");
+
+__global__ void k_noalloc_descs(const __grid_constant__ DescBlock blk, SegDev* dst) {
+    const int words = blk.count * (int)(sizeof(SegDev) / 4);
+    const int* src = reinterpret_cast<const int*>(blk.d);
+    int* out = reinterpret_cast<int*>(dst);
+    for (int w = threadIdx.x; w < words; w += blockDim.x) out[w] = src[w];
+}
+static_assert(sizeof(SegDev) % 4 == 0, "descriptors are copied in words");
 
 constexpr int MAX_DEVICES = 64;
 std::mutex g_setup_mu;
@@ -58,6 +76,15 @@ int scratch_for_current_device(unsigned char** out) {
     return GBNTT_OK;
 }
 
+// one persistent launch of the call, fully prepared before anything is enqueued
+struct PartLaunch {
+    const BatchConfig* cfg = nullptr;
+    int first = 0, count = 0;        // its descriptors in the block
+    long long tiles = 0;
+    int stage = 0, smem = 0;
+    long long grid = 0;
+};
+
 }  // namespace
 
 extern "C" int gbntt_batch_execute_noalloc(const gbntt_segment* segs, uint32_t nsegs, void* stream) {
@@ -71,9 +98,10 @@ extern "C" int gbntt_batch_execute_noalloc(const gbntt_segment* segs, uint32_t n
     int rc = scratch_for_current_device(&scratch);
     if (rc != GBNTT_OK) return rc;
 
-    // Descriptors on the stack: [0] int16 part, [1] int32 part.
-    SegDev desc[2][GBNTT_NOALLOC_MAX_SEGMENTS];
-    int nd[2] = {0, 0}, fam_mask[2] = {0, 0}, Ls[2][GBNTT_NOALLOC_MAX_SEGMENTS];
+    // 1. validate and sort every segment into its part (storage type and
+    //    arithmetic); segments without a persistent form run as plan launches
+    SegDev desc[BATCH_PARTS][GBNTT_NOALLOC_MAX_SEGMENTS];
+    int nd[BATCH_PARTS] = {}, fam_mask[BATCH_PARTS] = {}, Ls[BATCH_PARTS][GBNTT_NOALLOC_MAX_SEGMENTS];
     bool batched[GBNTT_NOALLOC_MAX_SEGMENTS] = {};
     for (uint32_t k = 0; k < nsegs; ++k) {
         const gbntt_segment& u = segs[k];
@@ -85,7 +113,7 @@ extern "C" int gbntt_batch_execute_noalloc(const gbntt_segment* segs, uint32_t n
         KArgs a;
         gbntt_internal_plan_args(u.plan, &fam, &L, &eb, &a);
         if (fam < 0 || !variant_supported(fam, L) || u.d_in == u.d_out) continue;   // runs as a plan launch
-        const int part = fam_i32(fam) ? 1 : 0;
+        const int part = batch_part_of(fam);
         SegDev& sd = desc[part][nd[part]];
         std::memset(&sd, 0, sizeof(sd));
         sd.a = a;
@@ -100,32 +128,32 @@ extern "C" int gbntt_batch_execute_noalloc(const gbntt_segment* segs, uint32_t n
         ++nd[part];
         batched[k] = true;
     }
-    // every call reuses the same scratch: the tile counters must start at zero
-    unsigned long long* ctr = reinterpret_cast<unsigned long long*>(scratch + NOALLOC_CTR_OFFSET);
-    cudaError_t e = cudaMemsetAsync(ctr, 0, 2 * CTR_WORDS * sizeof(unsigned long long), s);
-    if (e != cudaSuccess) return fail(GBNTT_ERR_CUDA, std::string("counter reset: ") + cudaGetErrorString(e));
+
+    // 2. choose every part's configuration, order its tiles and size its
+    //    launch; nothing is enqueued until all parts are ready
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    size_t desc_off = 0;
-    for (int part = 0; part < 2; ++part) {
+    DescBlock blk;
+    std::memset(&blk, 0, sizeof(blk));
+    PartLaunch pl[BATCH_PARTS];
+    for (int part = 0; part < BATCH_PARTS; ++part) {
         if (!nd[part]) continue;
+        PartLaunch& P = pl[part];
         // the narrowest compiled configuration covering these families and
-        // lengths, with the most resident CTAs among those (the choice the
-        // autotuner makes on the benchmark batch; the serving loop's rule)
+        // lengths, with the most resident CTAs among those (the serving loop's rule)
         const BatchConfig* cfgs = nullptr;
-        const int ncfg = part ? batch_configs_i32(&cfgs) : batch_configs_i16(&cfgs);
+        const int ncfg = (part & 1) ? batch_configs_i32(&cfgs) : batch_configs_i16(&cfgs);
         int maxL = 0;
         for (int i = 0; i < nd[part]; ++i) maxL = Ls[part][i] > maxL ? Ls[part][i] : maxL;
         auto resident = [](const BatchConfig& c) { return c.occ ? c.occ : batch_min_blocks(c.i32, c.cta, c.elmax); };
-        const BatchConfig* cfg = nullptr;
         for (int c = 0; c < ncfg; ++c)
             if (cfgs[c].cta == BATCH_CTA && (cfgs[c].set & fam_mask[part]) == fam_mask[part] &&
                 config_fits(cfgs[c], maxL) &&
-                (!cfg || cfgs[c].elmax < cfg->elmax ||
-                 (cfgs[c].elmax == cfg->elmax && resident(cfgs[c]) > resident(*cfg))))
-                cfg = &cfgs[c];
-        if (!cfg) return fail(GBNTT_ERR_ARG, "no persistent kernel covers these designs");
+                (!P.cfg || cfgs[c].elmax < P.cfg->elmax ||
+                 (cfgs[c].elmax == P.cfg->elmax && resident(cfgs[c]) > resident(*P.cfg))))
+                P.cfg = &cfgs[c];
+        if (!P.cfg) return fail(GBNTT_ERR_ARG, "no persistent kernel covers these designs");
         // tiles, largest n first
         int order[GBNTT_NOALLOC_MAX_SEGMENTS];
         for (int i = 0; i < nd[part]; ++i) order[i] = i;
@@ -133,43 +161,62 @@ extern "C" int gbntt_batch_execute_noalloc(const gbntt_segment* segs, uint32_t n
             for (int j = i; j > 0 && Ls[part][order[j]] > Ls[part][order[j - 1]]; --j) {
                 const int t = order[j]; order[j] = order[j - 1]; order[j - 1] = t;
             }
-        SegDev sorted[GBNTT_NOALLOC_MAX_SEGMENTS];
-        long long tiles = 0;
-        int stage = 0, xbytes = 0;
+        P.first = blk.count;
+        P.count = nd[part];
+        int xbytes = 0;
         for (int i = 0; i < nd[part]; ++i) {
             SegDev sd = desc[part][order[i]];
             const int L = Ls[part][order[i]];
-            const int G = 1 << (L - batch_el(L, cfg->elmax));
+            const int G = 1 << (L - batch_el(L, P.cfg->elmax));
             sd.polys_per_tile = BATCH_CTA / G;
             sd.tiles = (sd.a.batch + sd.polys_per_tile - 1) / sd.polys_per_tile;
-            sd.tile0 = tiles;
-            tiles += sd.tiles;
-            stage = stage > batch_stage_bytes(BATCH_CTA, L, sd.elem_bytes, cfg->elmax)
-                        ? stage : batch_stage_bytes(BATCH_CTA, L, sd.elem_bytes, cfg->elmax);
-            xbytes = xbytes > batch_xbuf_bytes(BATCH_CTA, L, cfg->elmax) ? xbytes
-                                                                          : batch_xbuf_bytes(BATCH_CTA, L, cfg->elmax);
-            sorted[i] = sd;
+            sd.tile0 = P.tiles;
+            P.tiles += sd.tiles;
+            const int st = batch_stage_bytes(BATCH_CTA, L, sd.elem_bytes, P.cfg->elmax);
+            const int xb = batch_xbuf_bytes(BATCH_CTA, L, P.cfg->elmax);
+            P.stage = P.stage > st ? P.stage : st;
+            xbytes = xbytes > xb ? xbytes : xb;
+            blk.d[blk.count++] = sd;
         }
-        stage = (stage + 127) & ~127;
-        const int smem = SMEM_HEADER + 2 * stage + xbytes;
-        SegDev* d_desc = reinterpret_cast<SegDev*>(scratch) + desc_off;
-        e = cudaMemcpyAsync(d_desc, sorted, sizeof(SegDev) * nd[part], cudaMemcpyHostToDevice, s);
-        if (e != cudaSuccess) return fail(GBNTT_ERR_CUDA, std::string("descriptor copy: ") + cudaGetErrorString(e));
-        desc_off += nd[part];
-        e = cudaFuncSetAttribute(cfg->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        P.stage = (P.stage + 127) & ~127;
+        P.smem = SMEM_HEADER + 2 * P.stage + xbytes;
+        cudaError_t e = raise_smem_limit(P.cfg->fn, P.smem);
         int per_sm = 0;
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cfg->fn, BATCH_CTA, smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, P.cfg->fn, BATCH_CTA, P.smem);
         if (e != cudaSuccess || per_sm < 1)
             return fail(GBNTT_ERR_CUDA, std::string("kernel configuration: ") + cudaGetErrorString(e));
+        P.grid = (long long)per_sm * sms < P.tiles ? (long long)per_sm * sms : P.tiles;
+    }
+
+    // 3. enqueue: descriptors, counter reset, the persistent launches, then
+    //    the plan launches
+    SegDev* d_desc = reinterpret_cast<SegDev*>(scratch);
+    unsigned long long* ctr = reinterpret_cast<unsigned long long*>(scratch + NOALLOC_CTR_OFFSET);
+    cudaError_t e = cudaSuccess;
+    if (blk.count) {
+        k_noalloc_descs<<<1, 256, 0, s>>>(blk, d_desc);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(GBNTT_ERR_CUDA, std::string("descriptors: ") + cudaGetErrorString(e));
+        gbntt_internal_count_launch();
+        // every call reuses the same counters: the tile counters (CTR_NEXT,
+        // CTR_DONE of each part) start at zero; the error words are kept
+        // until gbntt_noalloc_status reads them
+        e = cudaMemset2DAsync(ctr, CTR_WORDS * sizeof(unsigned long long), 0, 2 * sizeof(unsigned long long),
+                              BATCH_PARTS, s);
+        if (e != cudaSuccess) return fail(GBNTT_ERR_CUDA, std::string("counter reset: ") + cudaGetErrorString(e));
+    }
+    for (int part = 0; part < BATCH_PARTS; ++part) {
+        const PartLaunch& P = pl[part];
+        if (!P.count) continue;
         BatchDev bd;
-        bd.segs = d_desc;
-        bd.nsegs = nd[part];
-        bd.total_tiles = tiles;
+        bd.segs = d_desc + P.first;
+        bd.nsegs = P.count;
+        bd.total_tiles = P.tiles;
         bd.ctr = ctr + CTR_WORDS * part;
-        int sb = stage;
+        bd.wait_polls = batch_wait_polls();
+        int sb = P.stage;
         void* args[] = {&bd, &sb};
-        const long long grid = (long long)per_sm * sms < tiles ? (long long)per_sm * sms : tiles;
-        e = cudaLaunchKernel(cfg->fn, dim3((unsigned)grid), dim3(BATCH_CTA), args, smem, s);
+        e = cudaLaunchKernel(P.cfg->fn, dim3((unsigned)P.grid), dim3(BATCH_CTA), args, P.smem, s);
         if (e != cudaSuccess) return fail(GBNTT_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
         gbntt_internal_count_launch();
     }
@@ -179,4 +226,22 @@ extern "C" int gbntt_batch_execute_noalloc(const gbntt_segment* segs, uint32_t n
         if (rc != GBNTT_OK) return rc;
     }
     return GBNTT_OK;
+}
+
+extern "C" int gbntt_noalloc_status(void) {
+    unsigned char* scratch = nullptr;
+    const int rc = scratch_for_current_device(&scratch);
+    if (rc != GBNTT_OK) return rc;
+    unsigned long long* ctr = reinterpret_cast<unsigned long long*>(scratch + NOALLOC_CTR_OFFSET);
+    unsigned long long w[BATCH_PARTS * CTR_WORDS];
+    cudaError_t e = cudaMemcpy(w, ctr, sizeof(w), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(GBNTT_ERR_CUDA, std::string("status read: ") + cudaGetErrorString(e));
+    bool timed_out = false;
+    for (int p = 0; p < BATCH_PARTS; ++p) timed_out |= w[CTR_WORDS * p + CTR_ERROR] != 0;
+    if (!timed_out) return GBNTT_OK;
+    for (int p = 0; p < BATCH_PARTS; ++p) {
+        e = cudaMemset(ctr + CTR_WORDS * p + CTR_ERROR, 0, sizeof(unsigned long long));
+        if (e != cudaSuccess) return fail(GBNTT_ERR_CUDA, std::string("status reset: ") + cudaGetErrorString(e));
+    }
+    return fail(GBNTT_ERR_TIMEOUT, "a tile load of a no-alloc launch did not arrive within the wait limit");
 }

@@ -40,7 +40,12 @@ struct BatchDev {
     int nsegs;
     long long total_tiles;
     unsigned long long* ctr;   // CTR_WORDS scratch words, zero between launches
+    unsigned wait_polls;       // poll limit of a tile load's wait (BATCH_WAIT_POLLS; smaller in tests)
 };
+
+// The poll limit of every bounded wait: far beyond any real copy's latency,
+// short enough that a lost copy ends the launch with an error in seconds.
+constexpr unsigned BATCH_WAIT_POLLS = 1u << 22;
 
 // coefficients per thread (log2) of a persistent-kernel configuration
 __host__ __device__ constexpr int batch_el(int L, int elmax) { return L < elmax ? L : elmax; }
@@ -63,11 +68,12 @@ __device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned
                  : "memory");
 }
 
-// Bounded wait for the phase `parity` of the barrier.  Returns false when the
-// iteration limit ran out (the caller records an error and stops).
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+// Bounded wait for the phase `parity` of the barrier: at most `polls` polls.
+// Returns false when they ran out (the caller records an error and stops).
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity,
+                                          unsigned polls = BATCH_WAIT_POLLS) {
     const unsigned a = smem_addr(bar);
-    for (int it = 0; it < (1 << 22); ++it) {
+    for (unsigned it = 0; it < polls; ++it) {
         unsigned ok;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -153,9 +159,10 @@ __device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KC&
 #pragma unroll
         for (int k = 0; k < E; ++k) v[k] = 0;
     }
+    prologue<FAM>(v, ka);
     if constexpr (LO0 != LOS) exchange_windows<L, EL, LOS, LO0>(v, sp, g);
     run_steps<FAM, L, EL>(v, sp, g, a, std::make_integer_sequence<int, NS>{});
-    epilogue_all<fam_scales(FAM, false)>(v, ka);
+    epilogue<FAM, false>(v, ka);
     if (!active) return;
     if constexpr (fam_natural_out(FAM, false)) {
         if (ka.natural_out) {

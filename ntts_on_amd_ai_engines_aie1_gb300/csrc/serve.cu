@@ -186,12 +186,12 @@ struct Slot {
     // d_blk with one copy
     unsigned char* h_blk = nullptr;
     unsigned char* d_blk = nullptr;
-    unsigned long long* d_ctr = nullptr;   // tile counters of the two persistent launches
+    unsigned long long* d_ctr = nullptr;   // tile counters of the persistent launches (one per part)
     unsigned long long* h_err = nullptr;   // their error words (mapped), written by the scatter kernel
     unsigned long long* m_err = nullptr;   // device address of h_err
 };
 
-constexpr size_t ERR_BYTES = 2 * CTR_WORDS * sizeof(unsigned long long);
+constexpr size_t ERR_BYTES = BATCH_PARTS * CTR_WORDS * sizeof(unsigned long long);
 constexpr size_t BLK_ALIGN = 128;
 size_t blk_round(size_t b) { return (b + BLK_ALIGN - 1) / BLK_ALIGN * BLK_ALIGN; }
 
@@ -199,10 +199,10 @@ size_t blk_round(size_t b) { return (b + BLK_ALIGN - 1) / BLK_ALIGN * BLK_ALIGN;
 struct PlanInfo {
     int fam = -1, L = 0, eb = 0;
     gbntt::KArgs a;
-    int part = -1;   // 0 int16 / 1 int32 persistent launch, -1: the plan's own launches
+    int part = -1;   // persistent launch (batch_part_of), -1: the plan's own launches
 };
 
-// one persistent launch configuration per storage type
+// one persistent launch configuration per storage type and arithmetic
 struct PartCfg {
     const gbntt::BatchConfig* cfg = nullptr;
     int stage = 0, smem = 0, grid = 0;
@@ -214,7 +214,7 @@ struct gbntt_server {
     std::vector<const gbntt_plan*> plans;
     std::vector<int64_t> plan_bytes;   // bytes of one polynomial
     std::vector<PlanInfo> pinfo;
-    PartCfg part[2];
+    PartCfg part[BATCH_PARTS];
     std::vector<Slot> slots;
     Arena arena;
     char* d_arena = nullptr;
@@ -260,7 +260,9 @@ void set_worker_error(gbntt_server* s, int code, const std::string& msg) {
 
 void finish_slot(gbntt_server* s, Slot& sl) {
     const auto now = Clock::now();
-    if (sl.h_err[CTR_ERROR] || sl.h_err[CTR_WORDS + CTR_ERROR])   // a tile load ran out of its wait limit
+    bool timed_out = false;   // a tile load ran out of its wait limit
+    for (int p = 0; p < BATCH_PARTS; ++p) timed_out |= sl.h_err[CTR_WORDS * p + CTR_ERROR] != 0;
+    if (timed_out)
         set_worker_error(s, GBNTT_ERR_TIMEOUT, "serve: a tile load did not arrive within the wait limit");
     long long done = 0;
     std::lock_guard<std::mutex> lk(s->mu);
@@ -325,13 +327,17 @@ int issue(gbntt_server* s, Slot& sl) {
     std::stable_sort(order.begin(), order.end(), [&](const Group* x, const Group* y) {
         return s->pinfo[x->plan].L > s->pinfo[y->plan].L;
     });
-    int nseg[2] = {0, 0};
+    int nseg[BATCH_PARTS] = {};
     for (const Group* g : order)
         if (s->pinfo[g->plan].part >= 0) ++nseg[s->pinfo[g->plan].part];
     const size_t seg_off = blk_round((size_t)(nin + nout) * sizeof(CopyDesc));
     SegDev* segs = reinterpret_cast<SegDev*>(sl.h_blk + seg_off);
-    int fill[2] = {0, nseg[0]};
-    long long tiles[2] = {0, 0};
+    int first[BATCH_PARTS], fill[BATCH_PARTS], total_segs = 0;
+    for (int p = 0; p < BATCH_PARTS; ++p) {
+        first[p] = fill[p] = total_segs;
+        total_segs += nseg[p];
+    }
+    long long tiles[BATCH_PARTS] = {};
     for (const Group* g : order) {
         const PlanInfo& pi = s->pinfo[g->plan];
         if (pi.part < 0) continue;
@@ -349,7 +355,7 @@ int issue(gbntt_server* s, Slot& sl) {
         sd.tile0 = tiles[pi.part];
         tiles[pi.part] += sd.tiles;
     }
-    const size_t used = seg_off + (size_t)(nseg[0] + nseg[1]) * sizeof(SegDev);
+    const size_t used = seg_off + (size_t)total_segs * sizeof(SegDev);
     cudaError_t e = cudaMemcpyAsync(sl.d_blk, sl.h_blk, used, cudaMemcpyHostToDevice, sl.stream);
     if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve descriptors: ") + cudaGetErrorString(e));
     const CopyDesc* d_desc = reinterpret_cast<const CopyDesc*>(sl.d_blk);
@@ -374,10 +380,11 @@ int issue(gbntt_server* s, Slot& sl) {
     auto launch_part = [&](int p, cudaStream_t st) -> cudaError_t {
         const PartCfg& pc = s->part[p];
         BatchDev bd;
-        bd.segs = d_segs + (p ? nseg[0] : 0);
+        bd.segs = d_segs + first[p];
         bd.nsegs = nseg[p];
         bd.total_tiles = tiles[p];
         bd.ctr = sl.d_ctr + CTR_WORDS * p;
+        bd.wait_polls = batch_wait_polls();
         int sb = pc.stage;
         void* args[] = {&bd, &sb};
         const unsigned grid = (unsigned)std::min<long long>(pc.grid, tiles[p]);
@@ -388,17 +395,20 @@ int issue(gbntt_server* s, Slot& sl) {
         }
         return le;
     };
-    if (nseg[0] && nseg[1]) {
-        // the two launches share nothing but the gather before them
+    int used_parts[BATCH_PARTS], nparts = 0;
+    for (int p = 0; p < BATCH_PARTS; ++p)
+        if (nseg[p]) used_parts[nparts++] = p;
+    if (nparts >= 2) {
+        // the launches share nothing but the gather before them: the first on
+        // the slot's stream, the others beside it on the second stream
         e = cudaEventRecord(sl.fork, sl.stream);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(sl.aux, sl.fork, 0);
-        if (e == cudaSuccess) e = launch_part(1, sl.aux);
+        for (int i = 1; i < nparts && e == cudaSuccess; ++i) e = launch_part(used_parts[i], sl.aux);
         if (e == cudaSuccess) e = cudaEventRecord(sl.join, sl.aux);
-        if (e == cudaSuccess) e = launch_part(0, sl.stream);
+        if (e == cudaSuccess) e = launch_part(used_parts[0], sl.stream);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(sl.stream, sl.join, 0);
-    } else {
-        for (int p = 0; p < 2 && e == cudaSuccess; ++p)
-            if (nseg[p]) e = launch_part(p, sl.stream);
+    } else if (nparts == 1) {
+        e = launch_part(used_parts[0], sl.stream);
     }
     if (e != cudaSuccess) return sfail(GBNTT_ERR_CUDA, std::string("serve launch: ") + cudaGetErrorString(e));
     for (const Group* g : order) {
@@ -568,7 +578,7 @@ int gbntt_server_create(gbntt_server** out, const gbntt_plan* const* plans, uint
         s->plan_bytes.push_back(n * eb);
         PlanInfo pi;
         gbntt_internal_plan_args(p, &pi.fam, &pi.L, &pi.eb, &pi.a);
-        if (pi.fam >= 0 && variant_supported(pi.fam, pi.L)) pi.part = fam_i32(pi.fam) ? 1 : 0;
+        if (pi.fam >= 0 && variant_supported(pi.fam, pi.L)) pi.part = batch_part_of(pi.fam);
         s->pinfo.push_back(pi);
     }
     // per storage type: one persistent configuration covering the served families
@@ -576,7 +586,7 @@ int gbntt_server_create(gbntt_server** out, const gbntt_plan* const* plans, uint
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        for (int p = 0; p < 2; ++p) {
+        for (int p = 0; p < BATCH_PARTS; ++p) {
             int mask = 0, stage = 0, xbytes = 0, maxL = 0;
             for (const auto& pi : s->pinfo)
                 if (pi.part == p) {
@@ -585,7 +595,7 @@ int gbntt_server_create(gbntt_server** out, const gbntt_plan* const* plans, uint
                 }
             if (!mask) continue;
             const BatchConfig* cfgs = nullptr;
-            const int ncfg = p ? batch_configs_i32(&cfgs) : batch_configs_i16(&cfgs);
+            const int ncfg = (p & 1) ? batch_configs_i32(&cfgs) : batch_configs_i16(&cfgs);
             // the narrowest covering configuration (16 coefficients per thread
             // measured faster than 32 on mixed radix-4 batches), with the most
             // resident CTAs among those
@@ -613,7 +623,7 @@ int gbntt_server_create(gbntt_server** out, const gbntt_plan* const* plans, uint
             pc.stage = (stage + 127) & ~127;
             pc.smem = SMEM_HEADER + 2 * pc.stage + xbytes;
             int per_sm = 0;
-            cudaError_t e = cudaFuncSetAttribute(cfg->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pc.smem);
+            cudaError_t e = raise_smem_limit(cfg->fn, pc.smem);
             if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cfg->fn, BATCH_CTA, pc.smem);
             if (e != cudaSuccess || per_sm < 1) {
                 delete s;

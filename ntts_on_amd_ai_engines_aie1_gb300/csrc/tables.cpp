@@ -51,6 +51,30 @@ int log_root_order(int64_t q, int64_t root) {
     return -1;
 }
 
+bool canonical_fast(int kind, int64_t q, uint32_t flags) {
+    if (!(flags & FLAG_CANONICAL) || (flags & FLAG_LANE_EXACT)) return false;
+    switch (kind) {
+    case K_R2_I16_FWD: case K_R2_I16_INV: case K_R4_I16_FWD: case K_R4_I16_INV:
+        return true;
+    case K_R8_I16_FWD:
+        return !(flags & FLAG_R8_FLOAT);
+    case K_R2_I32_FWD: case K_R2_I32_INV:
+        return q < (1LL << 30);
+    default:
+        return false;
+    }
+}
+
+int canonical_family(int kind) {
+    switch (kind) {
+    case K_R2_I16_FWD: case K_R4_I16_FWD: case K_R8_I16_FWD: return 6;    // F_C16F
+    case K_R2_I16_INV: case K_R4_I16_INV: return 7;                       // F_C16I
+    case K_R2_I32_FWD: return 8;                                          // F_C32F
+    case K_R2_I32_INV: return 9;                                          // F_C32I
+    default: return -1;
+    }
+}
+
 uint32_t bitrev(uint32_t a, int bits) {
     uint32_t r = 0;
     for (int i = 0; i < bits; ++i) r |= ((a >> i) & 1u) << (bits - 1 - i);
@@ -179,8 +203,9 @@ int build_host_plan(int kind, uint32_t n, int64_t q, int64_t root, int64_t facto
         err = "natural order is not available for the two-pass int32 lengths (n >= 2^16)";
         return GBNTT_ERR_ARG;
     }
-    if ((flags & FLAG_SCALE_NINV) && !(kind == K_R2_I16_INV || kind == K_R4_I16_INV)) {
-        err = "the n^-1 epilogue applies to the int16 inverse designs only";
+    if ((flags & FLAG_SCALE_NINV) && !(kind == K_R2_I16_INV || kind == K_R4_I16_INV) &&
+        !(kind == K_R2_I32_INV && canonical_fast(kind, q, flags))) {
+        err = "the n^-1 epilogue applies to the int16 inverse designs (and to the canonical int32 inverse) only";
         return GBNTT_ERR_ARG;
     }
     (void)inverse;
@@ -327,7 +352,7 @@ int build_host_plan(int kind, uint32_t n, int64_t q, int64_t root, int64_t facto
         break;
     }
     }
-    if (flags & FLAG_SCALE_NINV) {
+    if ((flags & FLAG_SCALE_NINV) && !is32) {
         // the FULL_BARRETT_MULTIPLICATION<n, q, n^-1> unit fused after the inverse
         // (src/project.cpp:154, src/standalone_units.h:40)
         const int64_t ninv = modinv(n, q);

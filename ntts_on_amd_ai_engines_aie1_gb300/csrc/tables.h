@@ -24,6 +24,18 @@ constexpr uint32_t FLAG_R8_EXACT = 0x2u;
 constexpr uint32_t FLAG_R8_FLOAT = 0x4u;
 constexpr uint32_t FLAG_NATURAL_ORDER = 0x8u;
 constexpr uint32_t FLAG_SCALE_NINV = 0x10u;
+constexpr uint32_t FLAG_LANE_EXACT = 0x20u;
+
+// Largest two-pass (four-step) length of the canonical int32 family.
+constexpr int CANON_MAX_L32 = 22;
+
+// The plan runs a canonical family (Shoup multiplication, lazy lanes, one
+// final reduction): GBNTT_FLAG_CANONICAL without GBNTT_FLAG_LANE_EXACT on a
+// transform design (not the radix-8 single stage, not the radix-8 chain with
+// the reference's float multipliers), int32 moduli below 2^30.
+bool canonical_fast(int kind, int64_t q, uint32_t flags);
+// its family (F_C16F, F_C16I, F_C32F or F_C32I of device.cuh)
+int canonical_family(int kind);
 
 struct HostPlan {
     int kind = 0;

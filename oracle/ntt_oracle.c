@@ -780,3 +780,44 @@ void orc_dft(int n, int64_t q, int64_t root, int inverse, const int64_t* in, int
         out[k] = (int64_t)(acc % q);
     }
 }
+
+/* Exact transform in O(n log n), canonical residues: the iterative radix-2
+ * Cooley-Tukey algorithm of the textbooks (bit-reversal permutation, then
+ * log2 n layers of butterflies x +- w y mod q), with 64-bit products (q < 2^32).
+ * Forward: natural-order input, DFT with `root` in bit-reversed order (the
+ * order of every forward design of the reference); inverse: bit-reversed
+ * input, DFT with root^-1 in natural order, no n^-1 (the inverse designs'
+ * orders, README.md:157-160).  It restates no kernel of the reference: it is
+ * the mathematical transform those kernels compute, checked against orc_dft
+ * (the O(n^2) definition) in tests/test_oracle.py, and lets the tests check
+ * canonical outputs at lengths where the O(n^2) sum is too slow. */
+void orc_ntt_exact(int n, int64_t q, int64_t root, int inverse, const int64_t* in, int64_t* out) {
+    int L = 0;
+    while ((1 << L) < n) L++;
+    const uint64_t uq = (uint64_t)q;
+    const uint64_t w = (uint64_t)(inverse ? orc_modinv(root, q) : ((root % q) + q) % q);
+    /* textbook form: bit-reversed copy of the natural-order sequence, then
+     * butterflies of span 1, 2, 4, ... give the DFT in natural order */
+    uint64_t* a = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)n);
+    for (int i = 0; i < n; i++) {
+        /* the forward input is natural: permute it; the inverse input is
+         * already bit-reversed (it is a natural-order sequence permuted) */
+        const int src = inverse ? i : (int)orc_bitrev((uint32_t)i, L);
+        a[i] = (uint64_t)(((in[src] % q) + q) % q);
+    }
+    for (int m = 2; m <= n; m <<= 1) {
+        const uint64_t wm = (uint64_t)orc_powmod((int64_t)w, (uint64_t)(n / m), q);
+        for (int k = 0; k < n; k += m) {
+            uint64_t wj = 1;
+            for (int j = 0; j < m / 2; j++) {
+                const uint64_t t = wj * a[k + j + m / 2] % uq, u = a[k + j];
+                a[k + j] = (u + t) % uq;
+                a[k + j + m / 2] = (u + uq - t) % uq;
+                wj = wj * wm % uq;
+            }
+        }
+    }
+    /* natural order; the forward designs return bit-reversed order */
+    for (int i = 0; i < n; i++) out[i] = (int64_t)(inverse ? a[i] : a[orc_bitrev((uint32_t)i, L)]);
+    free(a);
+}

@@ -87,6 +87,11 @@ int orc_execute_mt(const orc_plan* p, const void* in, void* out, int64_t batch, 
 /* O(n^2) modular DFT, canonical residues.  out[k] = sum_j in[j] w^(+-jk). */
 void orc_dft(int n, int64_t q, int64_t root, int inverse, const int64_t* in, int64_t* out);
 
+/* Exact transform in O(n log n), canonical residues, in the designs' orders:
+ * forward = orc_dft(root) permuted to bit-reversed order; inverse = orc_dft
+ * with root^-1 of the bit-reversed input read back in natural order. */
+void orc_ntt_exact(int n, int64_t q, int64_t root, int inverse, const int64_t* in, int64_t* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -43,6 +43,8 @@ def lib():
                                      ctypes.c_int]
         L.orc_dft.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
                               ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_ntt_exact.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
+                                    ctypes.c_void_p, ctypes.c_void_p]
         for name, rt, at in [("orc_kyber_wq", ctypes.c_int16, [ctypes.c_int16, ctypes.c_int32]),
                              ("orc_r8_wq_float", ctypes.c_int32, [ctypes.c_int32, ctypes.c_int32]),
                              ("orc_r8_wq_exact", ctypes.c_int32, [ctypes.c_int32, ctypes.c_int32]),
@@ -107,6 +109,19 @@ def dft(x, q, root, inverse=False):
     y = np.empty_like(x)
     lib().orc_dft(x.size, q, root, int(inverse), x.ctypes.data, y.ctypes.data)
     return y
+
+
+def ntt_exact(x, q, root, inverse=False):
+    """The exact transform of every row of x (any integer dtype, taken mod q),
+    canonical residues as int64, in the designs' orders: forward natural in /
+    bit-reversed out, inverse bit-reversed in / natural out (no n^-1)."""
+    x = np.ascontiguousarray(x, dtype=np.int64)
+    n = x.shape[-1]
+    flat = x.reshape(-1, n)
+    out = np.empty_like(flat)
+    for r in range(flat.shape[0]):
+        lib().orc_ntt_exact(n, q, root, int(inverse), flat[r].ctypes.data, out[r].ctypes.data)
+    return out.reshape(x.shape)
 
 
 def bitrev_perm(n):

@@ -60,7 +60,9 @@ def test_mixed_batch(gb):
     xs = [torch.from_numpy(x).cuda() for _, x, _ in made]
     ys = [torch.full_like(x, 12345) for x in xs]
     b = gb.Batch([(p, x, y) for (p, _, _), x, y in zip(made, xs, ys)])
-    assert b.launches == 2 + 2          # int16 + int32 persistent launches, bitrev, r8 stage
+    # persistent launches: int16 and int32 lane arithmetic, the canonical int16
+    # segment's own; then the bit-reversal and radix-8 stage plan launches
+    assert b.launches == 3 + 2
     for rep in range(3):                # the tile counter re-arms itself
         for y in ys:
             y.fill_(12345)
@@ -148,3 +150,117 @@ def test_int32_batch_widths(gb, monkeypatch, Ls):
     torch.cuda.synchronize()
     for (_, _, y), w in zip(segs, wants):
         assert torch.equal(y, w)
+
+
+def _ragged_r8(gb, rng, flags, count=2000):
+    """The ragged radix-8 workload: `count` polynomials of n = 2^U, U uniform
+    in 8..12, q = 12289, natural-order output (bit reversal fused)."""
+    q = 12289
+    U = rng.integers(8, 13, count)
+    segs, xs = [], []
+    for L in range(8, 13):
+        n = 1 << L
+        c = int((U == L).sum())
+        plan = gb.Plan(8, n, q, pow(41, 4096 // n, q), 0, gb.FLAG_NATURAL_ORDER | flags)
+        x = rng.integers(0, q, (c, n)).astype(np.int16)
+        xs.append(x)
+        d = torch.from_numpy(x).cuda()
+        segs.append((plan, d, torch.full_like(d, 777)))
+    return segs, xs
+
+
+@pytest.mark.parametrize("canonical", [False, True])
+def test_ragged_radix8_natural_order_one_launch(gb, orc, canonical):
+    """2000 ragged radix-8 polynomials with the bit reversal fused, in ONE
+    persistent launch, every polynomial against the oracle's radix-8 chain
+    (exact multipliers) followed by its bit-reversal unit (reference:
+    src/kernels/ntt_r8_kernels.cc:214-404 then bitreverse_kernels.cc:54-143)."""
+    rng = np.random.default_rng(SEED + 30 + canonical)
+    segs, xs = _ragged_r8(gb, rng, gb.FLAG_CANONICAL if canonical else 0)
+    b = gb.Batch(segs)
+    assert b.launches == 1
+    b.execute()
+    torch.cuda.synchronize()
+    b.status()
+    q = 12289
+    for (plan, _, y), x in zip(segs, xs):
+        n = x.shape[1]
+        root = pow(41, 4096 // n, q)
+        want = orc.Plan(orc.R8_I16_FWD, n, q, root, r8_exact=True)(x)
+        bo = orc.Plan(orc.BITREV_I16, n)
+        want = bo(want)
+        if canonical:
+            want = want.astype(np.int64) % q
+            assert np.array_equal(want, orc.ntt_exact(x, q, root)[:, orc.bitrev_perm(n)])
+        assert np.array_equal(y.cpu().numpy().astype(np.int64), want.astype(np.int64)), n
+
+
+def test_canonical_batch_every_family(gb, orc):
+    """Canonical segments of both storage types and directions beside lane
+    segments: four persistent launches, each output against the exact transform
+    (canonical) or the oracle (lanes)."""
+    rng = np.random.default_rng(SEED + 40)
+    specs = [  # (kind, n, q, count, dtype, flags)
+        (2, 1024, 12289, 300, np.int16, 1), (0, 256, 7681, 201, np.int16, 1), (1, 4096, 12289, 7, np.int16, 1),
+        (9, 64, 12289, 99, np.int16, 1 | 0x10), (8, 512, 10753, 45, np.int16, 1 | 0x8),
+        (4, 8192, 998244353, 5, np.int32, 1), (5, 4096, 754974721, 19, np.int32, 1 | 0x10),
+        (4, 4, 469762049, 1000, np.int32, 1), (5, 1024, 167772161, 66, np.int32, 1 | 0x8),
+        (2, 256, 12289, 100, np.int16, 0), (4, 2048, 998244353, 9, np.int32, 0),
+    ]
+    segs, wants = [], []
+    for kind, n, q, count, dt, fl in specs:
+        root = root_for(q, n)
+        lo, hi = (-32768, 32768) if dt == np.int16 else (-(1 << 31), 1 << 31)
+        x = rng.integers(lo, hi, (count, n)).astype(dt) if fl & 1 else rng.integers(0, q, (count, n)).astype(dt)
+        d = torch.from_numpy(x).cuda()
+        segs.append((gb.Plan(kind, n, q, root, 0, fl), d, torch.full_like(d, 5)))
+        inverse = kind in (1, 5, 9)
+        if fl & 1:
+            xin = np.ascontiguousarray(x[:, orc.bitrev_perm(n)]) if (fl & 0x8 and inverse) else x
+            w = orc.ntt_exact(xin, q, root, inverse=inverse)
+            if fl & 0x10:
+                w = w * pow(n, -1, q) % q
+            if fl & 0x8 and not inverse:
+                w = w[:, orc.bitrev_perm(n)]
+        else:
+            w = orc.Plan(kind, n, q, root)(x)
+        wants.append(w)
+    b = gb.Batch(segs)
+    assert b.launches == 4
+    for rep in range(2):
+        b.graph_launch()
+        torch.cuda.synchronize()
+        b.status()
+        for i, ((_, _, y), w) in enumerate(zip(segs, wants)):
+            assert np.array_equal(y.cpu().numpy().astype(np.int64), w.astype(np.int64)), (i, rep)
+
+
+def test_bounded_wait_timeout_is_reported(gb):
+    """A tile load whose bounded wait runs out: the launch records
+    GBNTT_ERR_TIMEOUT (the CTA lets its copies in flight land and stops), the
+    status call reports and clears it, and the next launch is correct.  The
+    wait is made to run out by a limit of 0 polls, not by any fault."""
+    rng = np.random.default_rng(SEED + 50)
+    plan = gb.Plan(2, 1024, 12289, root_for(12289, 1024))
+    cplan = gb.Plan(4, 4096, 998244353, root_for(998244353, 4096), 0, gb.FLAG_CANONICAL)
+    x = torch.from_numpy(rng.integers(0, 12289, (2000, 1024)).astype(np.int16)).cuda()
+    x32 = torch.from_numpy(rng.integers(0, 998244353, (300, 4096)).astype(np.int32)).cuda()
+    y, y32 = torch.zeros_like(x), torch.zeros_like(x32)
+    b = gb.Batch([(plan, x, y), (cplan, x32, y32)])
+    want, want32 = plan(x), cplan(x32)
+    try:
+        gb.set_wait_limit(0)
+        b.execute()
+        torch.cuda.synchronize()
+        with pytest.raises(gb.NTTError) as err:
+            b.status()
+        assert err.value.code == 9              # GBNTT_ERR_TIMEOUT
+    finally:
+        gb.set_wait_limit()
+    b.status()                                  # the error was cleared by the report
+    y.zero_()
+    y32.zero_()
+    b.execute()
+    torch.cuda.synchronize()
+    b.status()
+    assert torch.equal(y, want) and torch.equal(y32, want32)

@@ -214,3 +214,20 @@ def test_full_barrett(orc):
     y = orc.Plan(orc.FULL_BARRETT_I16, n, q, 0, factor=F)(x.astype(np.int16)).astype(np.int64)
     assert np.array_equal(y % q, F * x % q)
     assert y.min() >= 0 and y.max() <= q
+
+
+@pytest.mark.parametrize("q,g,n", [(12289, 11, 256), (7681, 17, 512), (998244353, 3, 128),
+                                   (1073707009, 0, 64), (469762049, 3, 2)])
+def test_exact_transform_is_the_dft(orc, q, g, n):
+    """oracle.ntt_exact (the canonical families' checker) against the O(n^2)
+    definition: forward in bit-reversed order, inverse from bit-reversed input,
+    and the round trip returns n x."""
+    root = pow(992735929, 2048 // n, q) if g == 0 else pow(g, (q - 1) // n, q)
+    rng = np.random.default_rng(n + q % 101)
+    x = rng.integers(-(1 << 31), 1 << 31, (3, n))
+    br = orc.bitrev_perm(n)
+    f = orc.ntt_exact(x, q, root)
+    assert np.array_equal(f, np.stack([orc.dft(r, q, root) for r in x])[:, br])
+    i = orc.ntt_exact(f, q, root, inverse=True)
+    assert np.array_equal(i, np.stack([orc.dft(r[br], q, root, inverse=True) for r in f]))
+    assert np.array_equal(i, (x % q) * n % q)
