@@ -38,11 +38,33 @@ WORKLOAD = ("batched radix-4 int16 forward NTT: 4096 polys x 4 moduli {7681,1075
             "n=256 for 7681/10753 (no 1024-th root of unity), n=1024 for 12289")
 
 
-def workload_config():
-    """The workload part of the JSON line's config, shared by both arms."""
-    return {"workload": WORKLOAD, "polys_per_step": sum(cnt for _, _, cnt, _ in SEGMENTS),
+OUTPUTS = {
+    "canonical": "canonical residues in [0, q): the reference's outputs reduced mod q (its lanes do not wrap "
+                 "on this workload), i.e. the forward DFT in bit-reversed order",
+    "lanes": "the reference's partially reduced int16 outputs, bit for bit",
+}
+
+
+def workload_config(arith, gpus):
+    """The JSON line's config: identical in both arms (same keys, same values)."""
+    return {"workload": WORKLOAD, "outputs": OUTPUTS[arith], "polys_per_step": sum(cnt for _, _, cnt, _ in SEGMENTS),
             "coefficients_per_step": sum(n * cnt for _, n, cnt, _ in SEGMENTS),
-            "algorithmic_bytes_per_step": sum(2 * n * 2 * cnt for _, n, cnt, _ in SEGMENTS)}
+            "algorithmic_bytes_per_step": sum(2 * n * 2 * cnt for _, n, cnt, _ in SEGMENTS),
+            "l2": "flushed before every step (256 MiB write, untimed); the CPU arm times host memory",
+            "parallelism": f"replicas{gpus}"}
+
+
+def coeffs_per_poly():
+    return sum(n * cnt for _, n, cnt, _ in SEGMENTS) / sum(cnt for _, _, cnt, _ in SEGMENTS)
+
+
+def oracle_outputs(oracle, x, q, n, g, arith, threads=1):
+    """The reference's algorithm (the oracle's restatement) on x; reduced mod q
+    for canonical outputs."""
+    y = oracle.Plan(oracle.R4_I16_FWD, n, q, root_of(q, n, g))(x, threads=threads)
+    if arith == "canonical":
+        y = np.mod(y, q, dtype=np.int16) if y.dtype == np.int16 else np.mod(y, q)
+    return y
 
 
 def max_over_ranks(x, dist=None, device="cpu"):
@@ -152,15 +174,14 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(inside), "note": note}
 
 
-def cpu_baseline(inputs, seconds, threads):
+def cpu_baseline(inputs, seconds, threads, arith):
     """The oracle (CPU restatement of the reference's loops) over all host threads,
-    whole batches until `seconds` have passed."""
+    whole batches until `seconds` have passed (reduced mod q for canonical outputs)."""
     from oracle import oracle
-    plans = [oracle.Plan(oracle.R4_I16_FWD, n, q, root_of(q, n, g)) for (q, n, _, g) in SEGMENTS]
     done, t0 = 0, time.perf_counter()
     while True:
-        for p, x in zip(plans, inputs):
-            p(x, threads=threads)
+        for (q, n, _, g), x in zip(SEGMENTS, inputs):
+            oracle_outputs(oracle, x, q, n, g, arith, threads)
         done += sum(x.shape[0] for x in inputs)
         el = time.perf_counter() - t0
         if el >= seconds:
@@ -175,11 +196,13 @@ def run_reference(args):
     threads = host_threads()
     inputs = make_inputs()
     from oracle import oracle
-    plans = [oracle.Plan(oracle.R4_I16_FWD, n, q, root_of(q, n, g)) for (q, n, _, g) in SEGMENTS]
+
+    def step(xs):
+        for (q, n, _, g), x in zip(SEGMENTS, xs):
+            oracle_outputs(oracle, x, q, n, g, args.arith, threads)
     # size each step so that warmup + steps stay within about two minutes
     t0 = time.perf_counter()
-    for p, x in zip(plans, inputs):
-        p(x, threads=threads)
+    step(inputs)
     full = time.perf_counter() - t0
     budget = 120.0
     frac = 1.0
@@ -188,13 +211,11 @@ def run_reference(args):
     sample = [x[: max(1, int(x.shape[0] * frac))] for x in inputs]
     per_step = sum(s.shape[0] for s in sample)
     for _ in range(args.warmup):
-        for p, x in zip(plans, sample):
-            p(x, threads=threads)
+        step(sample)
     times = []
     for _ in range(args.steps):
         t = time.perf_counter()
-        for p, x in zip(plans, sample):
-            p(x, threads=threads)
+        step(sample)
         times.append(time.perf_counter() - t)
     ms = 1e3 * sum(times) / len(times)
     value = per_step / (ms / 1e3)
@@ -203,11 +224,12 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "NTT/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int16", "data": "synthetic",
-        "config": {**workload_config(), "parallelism": f"replicas{args.gpus}",
-                   "sampled_polys_per_step": per_step},
+        "config": workload_config(args.arith, args.gpus),
+        "coefficients_per_s": value * coeffs_per_poly(),
         "cpu_baseline": {"value": value, "unit": "NTT/s", "cores": threads, "kind": "port",
                          "sample": desc + "; the reference's AIE kernels cannot be built here, so its CPU "
-                                          "restatement (oracle/ntt_oracle.c, the parity oracle) is timed"},
+                                          "restatement (oracle/ntt_oracle.c, the parity oracle) is timed"
+                                          + ("; outputs reduced mod q" if args.arith == "canonical" else "")},
         "e2e": {"value": value, "unit": "NTT/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -229,7 +251,8 @@ def run_ours(args):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     inputs = make_inputs()
-    plans = [gb.Plan(gb.Kind.R4_I16_FWD, n, q, root_of(q, n, g)) for (q, n, _, g) in SEGMENTS]
+    flags = gb.FLAG_CANONICAL if args.arith == "canonical" else 0
+    plans = [gb.Plan(gb.Kind.R4_I16_FWD, n, q, root_of(q, n, g), 0, flags) for (q, n, _, g) in SEGMENTS]
     d_in = [torch.from_numpy(x).to(dev) for x in inputs]
     d_out = [torch.empty_like(x) for x in d_in]
     batch = gb.Batch([(plans[i], d_in[i], d_out[i]) for i in range(len(SEGMENTS))])
@@ -242,9 +265,11 @@ def run_ours(args):
     batch.execute(stream)
     torch.cuda.synchronize()
     batch.status()
+    want_out = []
     for i, (q, n, _, g) in enumerate(SEGMENTS):
-        want = oracle.Plan(oracle.R4_I16_FWD, n, q, root_of(q, n, g))(inputs[i], threads=host_threads())
+        want = oracle_outputs(oracle, inputs[i], q, n, g, args.arith, host_threads())
         assert np.array_equal(d_out[i].cpu().numpy(), want), "GPU output differs from the oracle"
+        want_out.append(want)
 
     def timed(run, steps):
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -317,9 +342,8 @@ def run_ours(args):
             batch.execute_host(h_in, h_out, stream)
             e2e_t.append(time.perf_counter() - t0)
         e2e_ms = max_over_ranks(1e3 * sum(e2e_t) / len(e2e_t), dist, dev)   # whole job: slowest rank
-        for i, (q, n, _, g) in enumerate(SEGMENTS):
-            want = oracle.Plan(oracle.R4_I16_FWD, n, q, root_of(q, n, g))(inputs[i][:128])
-            assert np.array_equal(h_out[i][:128].numpy(), want)
+        for i in range(len(SEGMENTS)):
+            assert np.array_equal(h_out[i].numpy(), want_out[i]), "end-to-end output differs from the oracle"
         e2e = {"value": whole_job_value(polys, world, e2e_ms), "unit": "NTT/s",
                "h2d_bytes_per_step": world * algo_bytes // 2, "d2h_bytes_per_step": world * algo_bytes // 2,
                "ms_per_step": e2e_ms, "steps": e2e_steps,
@@ -328,7 +352,7 @@ def run_ours(args):
 
     configs = None
     if rank == 0 and not args.skip_configs:
-        configs = run_configs(gb, oracle, flush, stream, peak)
+        configs = run_configs(gb, oracle, flush, stream, peak, args.arith)
 
     serving = None
     if rank == 0 and not args.skip_serve:
@@ -341,24 +365,28 @@ def run_ours(args):
     threads = host_threads()
     cpu = None
     if not args.skip_cpu:
-        v, done, el = cpu_baseline(inputs, args.cpu_seconds, threads)
+        v, done, el = cpu_baseline(inputs, args.cpu_seconds, threads, args.arith)
         cpu = {"value": v, "unit": "NTT/s", "cores": threads, "kind": "port",
                "sample": f"{done} NTTs of the same workload in {el:.1f} s (whole batches), oracle/ntt_oracle.c "
-                         f"with {threads} threads; the reference's AIE kernels cannot be built here"}
+                         f"with {threads} threads; the reference's AIE kernels cannot be built here"
+                         + ("; outputs reduced mod q" if args.arith == "canonical" else "")}
+    tr = (traffic or {}).get("headline_" + args.arith) or {}
     line = {
         "metric": METRIC, "value": value, "unit": "NTT/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int16", "data": "synthetic",
-        "config": {**workload_config(), "launch": "one persistent kernel, CUDA graph replay",
-                   "autotuned_log2_coeffs_per_thread": batch.query(4), "autotuned_cta_threads": batch.query(6),
-                   "l2": "flushed before every step (256 MiB write, untimed)", "parallelism": f"replicas{world}"},
+        "config": workload_config(args.arith, world),
+        "coefficients_per_s": value * coeffs_per_poly(),
+        "run": {"launch": "one persistent kernel, CUDA graph replay", "arithmetic": args.arith,
+                "autotuned_log2_coeffs_per_thread": batch.query(4), "autotuned_cta_threads": batch.query(6)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src,
-                     "kernel": "k_batch<int16> persistent radix-4 (all 16384 polys per launch)",
+                     "kernel": f"k_batch<int16> persistent radix-4 ({args.arith} arithmetic, all 16384 polys "
+                               "per launch)",
                      "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_ms": ms,
-                     "traffic": (traffic or {}).get("bytes_per_launch"),
+                     "traffic": tr.get("bytes_per_launch"),
                      # the bound that holds: integer issue (ncu capture of the same kernel)
-                     "issue": {k: (traffic or {}).get(k) for k in
+                     "issue": {k: tr.get(k) for k in
                                ("issue_active_frac", "alu_pipe_frac", "thread_instructions_per_coefficient")}},
         "cpu_baseline": cpu,
         "e2e": e2e,
@@ -373,21 +401,28 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def run_configs(gb, oracle, flush, stream, peak):
+def run_configs(gb, oracle, flush, stream, peak, arith):
     """The other workloads, measured beside the headline (device-resident
-    inputs, L2 flushed before each timed launch, CUDA events on the stream):
-    C1 radix-2 int16 forward then inverse, n = 1024, one polynomial (latency);
-    C2 radix-2 int32 forward + inverse, n = 4096, 1024 polynomials for each of
-    four primes (one persistent launch per direction); C4a ragged radix-8 int16 forward with the bit reversal fused
-    (natural-order output), 2000 polynomials of n = 2^U, U uniform in {8..12},
-    one persistent launch; C4b radix-2 int32 forward and inverse of 64
-    polynomials of n = 2^20 (two-pass schedule).  Each is checked against the
-    oracle on a sample first."""
+    inputs, L2 flushed before each timed launch, CUDA events on the stream,
+    median of the timed launches), each checked against the oracle first (the
+    reference's lanes) or the exact transform (canonical residues):
+      C3 twin: the headline batch in the other arithmetic;
+      C1: radix-2 int16 forward then inverse, n = 1024, one polynomial (latency);
+      C2: radix-2 int32 forward + inverse, n = 4096, 1024 polynomials for each
+          of four primes (one persistent launch per direction);
+      C4a: ragged radix-8 int16 forward with the bit reversal fused, 2000
+          polynomials of n = 2^U, U uniform in {8..12}, one persistent launch;
+      C4b: int32 forward and inverse of 64 polynomials of n = 2^20, q = 998244353
+          (canonical: the TMA-fed four-step; lanes: the two-pass schedule);
+      C16k: int32 forward and inverse of 4096 polynomials of n = 2^14.
+    Entries for n >= 2^14 carry a roofline object like the headline's."""
     import torch
 
     dev = torch.device("cuda")
     rng = np.random.default_rng(SEED + 2)
+    traffic = load_traffic() or {}
     out = {}
+    CAN = gb.FLAG_CANONICAL
 
     def timed(fn, steps):
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -401,91 +436,142 @@ def run_configs(gb, oracle, flush, stream, peak):
         torch.cuda.synchronize()
         return statistics.median([a.elapsed_time(b) for a, b in evs])
 
-    # C1
+    def entry(ntts, coefs, nbytes, ms, launches, **kw):
+        e = {"NTT_per_s": ntts / (ms / 1e3), "coefficients_per_s": coefs / (ms / 1e3),
+             "GBps": nbytes / (ms / 1e3) / 1e9, "frac_of_hbm": nbytes / (ms / 1e3) / 1e9 / peak, "ms": ms,
+             "launches": launches}
+        e.update(kw)
+        return e
+
+    def roofline(key, nbytes, ms, kernel):
+        achieved = nbytes / (ms / 1e3) / 1e9
+        tr = traffic.get(key) or {}
+        return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "kernel": kernel, "algorithmic_bytes_per_launch": nbytes, "avg_launch_ms": ms,
+                "traffic": tr.get("bytes_per_launch"), "traffic_note": tr.get("note")}
+
+    # C3 in the other arithmetic
+    other = "lanes" if arith == "canonical" else "canonical"
+    fl = CAN if other == "canonical" else 0
+    xs = make_inputs()
+    segs = []
+    for (q, n, cnt, g), x in zip(SEGMENTS, xs):
+        d = torch.from_numpy(x).to(dev)
+        segs.append((gb.Plan(gb.Kind.R4_I16_FWD, n, q, root_of(q, n, g), 0, fl), d, torch.empty_like(d)))
+    b3 = gb.Batch(segs)
+    b3.execute(stream)
+    torch.cuda.synchronize()
+    for (q, n, _, g), x, (_, _, y) in zip(SEGMENTS, xs, segs):
+        assert np.array_equal(y.cpu().numpy(), oracle_outputs(oracle, x, q, n, g, other, host_threads())), "C3"
+    ms = timed(lambda: b3.graph_launch(stream), 200)
+    polys = sum(c for _, _, c, _ in SEGMENTS)
+    coefs = sum(n * c for _, n, c, _ in SEGMENTS)
+    out[f"C3_{other}"] = entry(polys, coefs, 4 * coefs, ms, b3.launches, outputs=OUTPUTS[other])
+    del b3, segs
+
+    # C1: latency of one forward + inverse pair
     q, n = 12289, 1024
     root = pow(41, 4, q)
-    f = gb.Plan(gb.Kind.R2_I16_FWD, n, q, root)
-    i = gb.Plan(gb.Kind.R2_I16_INV, n, q, root)
     x = rng.integers(0, q, (1, n)).astype(np.int16)
     dx = torch.from_numpy(x).to(dev)
-    y = torch.empty_like(dx)
-    z = torch.empty_like(dx)
-    f.execute(dx, y, 1, stream)
-    i.execute(y, z, 1, stream)
-    torch.cuda.synchronize()
-    assert np.array_equal(y.cpu().numpy(), oracle.Plan(oracle.R2_I16_FWD, n, q, root)(x))
-    assert np.array_equal(z.cpu().numpy() % q, (x.astype(np.int64) * n) % q)
-    ms = timed(lambda: (f.execute(dx, y, 1, stream), i.execute(y, z, 1, stream)), 200)
-    out["C1_r2_i16_fwd_inv_n1024"] = {"us_per_fwd_inv_pair": ms * 1e3, "launches": 2}
-
-    # C2: the four primes' forward transforms as one persistent launch, then the inverses as another
-    n, cnt = 4096, 1024
-    fwd_segs, inv_segs, xs = [], [], []
-    for qq, g in SERVE_Q32:
-        root = pow(g, (qq - 1) // n, qq)
-        x = rng.integers(0, qq, (cnt, n)).astype(np.int32)
-        dx = torch.from_numpy(x).to(dev)
+    for name, fl in (("lanes", 0), ("canonical", CAN)):
+        f = gb.Plan(gb.Kind.R2_I16_FWD, n, q, root, 0, fl)
+        i = gb.Plan(gb.Kind.R2_I16_INV, n, q, root, 0, fl)
         y, z = torch.empty_like(dx), torch.empty_like(dx)
-        fwd_segs.append((gb.Plan(gb.Kind.R2_I32_FWD, n, qq, root), dx, y))
-        inv_segs.append((gb.Plan(gb.Kind.R2_I32_INV, n, qq, root), y, z))
-        xs.append((x, qq, root))
-    bf, bi = gb.Batch(fwd_segs), gb.Batch(inv_segs)
-    bf.execute(stream)
-    bi.execute(stream)
-    torch.cuda.synchronize()
-    for (x, qq, root), (_, _, y), (_, _, z) in zip(xs, fwd_segs, inv_segs):
-        assert np.array_equal(y[:4].cpu().numpy(), oracle.Plan(oracle.R2_I32_FWD, n, qq, root)(x[:4])), "C2"
-        assert np.array_equal(z[:4].cpu().numpy().astype(np.int64) % qq, (x[:4].astype(np.int64) * n) % qq), "C2"
-    tot_ms = timed(lambda: (bf.graph_launch(stream), bi.graph_launch(stream)), 50)
-    b = 4 * 2 * cnt * 2 * n * 4
-    out["C2_r2_i32_fwd_inv_n4096_4primes"] = {"NTT_per_s": 4 * 2 * cnt / (tot_ms / 1e3), "GBps": b / (tot_ms / 1e3) / 1e9,
-                                             "frac_of_hbm": b / (tot_ms / 1e3) / 1e9 / peak, "ms": tot_ms,
-                                             "launches": 2}
+        f.execute(dx, y, 1, stream)
+        i.execute(y, z, 1, stream)
+        torch.cuda.synchronize()
+        want = oracle.Plan(oracle.R2_I16_FWD, n, q, root)(x)
+        assert np.array_equal(y.cpu().numpy(), want % q if fl else want), "C1"
+        assert np.array_equal(z.cpu().numpy().astype(np.int64) % q, (x.astype(np.int64) * n) % q), "C1"
+        ms = timed(lambda: (f.execute(dx, y, 1, stream), i.execute(y, z, 1, stream)), 200)
+        out[f"C1_r2_i16_fwd_inv_n1024_{name}"] = {"us_per_fwd_inv_pair": ms * 1e3, "launches": 2}
 
-    # C4a
+    # C2: the four primes' forward transforms as one persistent launch, then the inverses
+    n, cnt = 4096, 1024
+    for name, fl in (("canonical", CAN), ("lanes", 0)):
+        fwd_segs, inv_segs, keep = [], [], []
+        for qq, g in SERVE_Q32:
+            root = pow(g, (qq - 1) // n, qq)
+            x = rng.integers(0, qq, (cnt, n)).astype(np.int32)
+            dx = torch.from_numpy(x).to(dev)
+            y, z = torch.empty_like(dx), torch.empty_like(dx)
+            fwd_segs.append((gb.Plan(gb.Kind.R2_I32_FWD, n, qq, root, 0, fl), dx, y))
+            inv_segs.append((gb.Plan(gb.Kind.R2_I32_INV, n, qq, root, 0, fl), y, z))
+            keep.append((x, qq, root))
+        bf, bi = gb.Batch(fwd_segs), gb.Batch(inv_segs)
+        bf.execute(stream)
+        bi.execute(stream)
+        torch.cuda.synchronize()
+        for (x, qq, root), (_, _, y), (_, _, z) in zip(keep, fwd_segs, inv_segs):
+            want = oracle.Plan(oracle.R2_I32_FWD, n, qq, root)(x[:4])
+            assert np.array_equal(y[:4].cpu().numpy(), want % qq if fl else want), "C2"
+            assert np.array_equal(z[:4].cpu().numpy().astype(np.int64) % qq, (x[:4].astype(np.int64) * n) % qq), "C2"
+        ms = timed(lambda: (bf.graph_launch(stream), bi.graph_launch(stream)), 50)
+        nb = 4 * 2 * cnt * 2 * n * 4
+        out[f"C2_r2_i32_fwd_inv_n4096_4primes_{name}"] = entry(8 * cnt, 8 * cnt * n, nb, ms, 2)
+        del bf, bi, fwd_segs, inv_segs
+
+    # C4a: ragged radix-8, natural-order output, one persistent launch
     q = 12289
     U = rng.integers(8, 13, 2000)
-    segs, keep, algo = [], [], 0
-    for L in range(8, 13):
-        c = int((U == L).sum())
-        n = 1 << L
-        p = gb.Plan(gb.Kind.R8_I16_FWD, n, q, pow(41, 4096 // n, q), flags=gb.FLAG_NATURAL_ORDER)
-        x = rng.integers(0, q, (c, n)).astype(np.int16)
-        dx = torch.from_numpy(x).to(dev)
-        dy = torch.empty_like(dx)
-        segs.append((p, dx, dy))
-        keep.append((x, dy, n))
-        algo += 2 * 2 * n * c
-    batch = gb.Batch(segs)
-    batch.execute(stream)
-    torch.cuda.synchronize()
-    for x, dy, n in keep:
-        want = oracle.Plan(oracle.R8_I16_FWD, n, q, pow(41, 4096 // n, q), r8_exact=True)(x[:8])[:, oracle.bitrev_perm(n)]
-        assert np.array_equal(dy[:8].cpu().numpy(), want), "C4a differs from the oracle"
-    ms = timed(lambda: batch.graph_launch(stream), 200)
-    out["C4a_ragged_r8_i16_natural_2000"] = {"NTT_per_s": 2000 / (ms / 1e3), "GBps": algo / (ms / 1e3) / 1e9,
-                                            "frac_of_hbm": algo / (ms / 1e3) / 1e9 / peak, "us": ms * 1e3,
-                                            "launches": batch.query(0)}
+    for name, fl in (("canonical", CAN), ("lanes", 0)):
+        segs, keep, algo, coefs = [], [], 0, 0
+        for L in range(8, 13):
+            c = int((U == L).sum())
+            n = 1 << L
+            p = gb.Plan(gb.Kind.R8_I16_FWD, n, q, pow(41, 4096 // n, q), 0, gb.FLAG_NATURAL_ORDER | fl)
+            x = rng.integers(0, q, (c, n)).astype(np.int16)
+            dx = torch.from_numpy(x).to(dev)
+            dy = torch.empty_like(dx)
+            segs.append((p, dx, dy))
+            keep.append((x, dy, n))
+            algo += 2 * 2 * n * c
+            coefs += n * c
+        batch = gb.Batch(segs)
+        batch.execute(stream)
+        torch.cuda.synchronize()
+        for x, dy, n in keep:
+            want = oracle.Plan(oracle.R8_I16_FWD, n, q, pow(41, 4096 // n, q), r8_exact=True)(x[:8])
+            want = want[:, oracle.bitrev_perm(n)]
+            assert np.array_equal(dy[:8].cpu().numpy(), want % q if fl else want), "C4a"
+        ms = timed(lambda: batch.graph_launch(stream), 200)
+        out[f"C4a_ragged_r8_i16_natural_2000_{name}"] = entry(2000, coefs, algo, ms, batch.query(0), us=ms * 1e3)
+        del batch, segs
 
-    # C4b
-    q, n, cnt = 998244353, 1 << 20, 64
-    root = 565042129
-    f = gb.Plan(gb.Kind.R2_I32_FWD, n, q, root)
-    i = gb.Plan(gb.Kind.R2_I32_INV, n, q, root)
-    x = rng.integers(0, q, (cnt, n)).astype(np.int32)
-    dx = torch.from_numpy(x).to(dev)
-    y = torch.empty_like(dx)
-    z = torch.empty_like(dx)
-    f.execute(dx, y, cnt, stream)
-    i.execute(y, z, cnt, stream)
-    torch.cuda.synchronize()
-    assert np.array_equal(y[:1].cpu().numpy(), oracle.Plan(oracle.R2_I32_FWD, n, q, root)(x[:1]))
-    assert np.array_equal(z[:2].cpu().numpy().astype(np.int64) % q, (x[:2].astype(np.int64) * n) % q)
-    b = 2 * n * 4 * cnt
-    for name, pl, src, dst in (("fwd", f, dx, y), ("inv", i, y, z)):
-        ms = timed(lambda: pl.execute(src, dst, cnt, stream), 20)
-        out[f"C4b_r2_i32_{name}_n2^20_64"] = {"NTT_per_s": cnt / (ms / 1e3), "GBps": b / (ms / 1e3) / 1e9,
-                                             "frac_of_hbm": b / (ms / 1e3) / 1e9 / peak, "ms": ms}
+    # C4b and C16k: int32 n >= 2^14, forward and inverse
+    for tag, L, cnt in (("C4b", 20, 64), ("C16k", 14, 4096)):
+        q = 998244353
+        n = 1 << L
+        root = pow(3, (q - 1) >> L, q)
+        x = rng.integers(0, q, (cnt, n)).astype(np.int32)
+        dx = torch.from_numpy(x).to(dev)
+        y, z = torch.empty_like(dx), torch.empty_like(dx)
+        nb = 2 * n * 4 * cnt
+        for name, fl in (("canonical", CAN), ("lanes", 0)):
+            f = gb.Plan(gb.Kind.R2_I32_FWD, n, q, root, 0, fl)
+            i = gb.Plan(gb.Kind.R2_I32_INV, n, q, root, 0, fl)
+            f.execute(dx, y, cnt, stream)
+            i.execute(y, z, cnt, stream)
+            torch.cuda.synchronize()
+            f.status()
+            i.status()
+            if fl:
+                assert np.array_equal(y[:1].cpu().numpy().astype(np.int64), oracle.ntt_exact(x[:1], q, root)), tag
+            else:
+                assert np.array_equal(y[:1].cpu().numpy(), oracle.Plan(oracle.R2_I32_FWD, n, q, root)(x[:1])), tag
+            assert np.array_equal(z[:2].cpu().numpy().astype(np.int64) % q, (x[:2].astype(np.int64) * n) % q), tag
+            for d, pl, src, dst in (("fwd", f, dx, y), ("inv", i, y, z)):
+                c0 = gb.launch_count()
+                pl.execute(src, dst, cnt, stream)
+                launches = gb.launch_count() - c0
+                ms = timed(lambda: pl.execute(src, dst, cnt, stream), 20)
+                key = f"{tag}_r2_i32_{d}_n2^{L}_{cnt}_{name}"
+                out[key] = entry(cnt, cnt * n, nb, ms, launches)
+                if fl:
+                    kern = ("four-step: k_ccols (TMA column pass) + k_crows (twist, row pass)" if L >= 16
+                            else "k_ntt (one CTA per polynomial)")
+                    out[key]["roofline"] = roofline(key, nb, ms, kern)
     return out
 
 
@@ -608,11 +694,15 @@ PROFILE_CASES = {
     "c_r2f32_16k": (4, 1 << 14, 998244353, 666702199, 4096, 1),
     "c_r2g32_16k": (5, 1 << 14, 998244353, 666702199, 4096, 1),
     "c_r2f32_32k": (4, 1 << 15, 998244353, pow(3, (998244353 - 1) >> 15, 998244353), 2048, 1),
+    "c_r2f32_1m": (4, 1 << 20, 998244353, 565042129, 64, 1),
+    "c_r2g32_1m": (5, 1 << 20, 998244353, 565042129, 64, 1),
+    "c_r2f32_64k": (4, 1 << 16, 998244353, pow(3, (998244353 - 1) >> 16, 998244353), 1024, 1),
     "batch_r4": None,   # the benchmark batch, 4x larger, persistent kernel
+    "c_batch_r4": None,  # the same with GBNTT_FLAG_CANONICAL
 }
 
 
-def run_profile_batch(scale=4, launches=3):
+def run_profile_batch(scale=4, launches=3, flags=0):
     """The benchmark's batch with every segment `scale` times larger (inputs
     larger than L2), executed `launches` times as one persistent launch."""
     import torch
@@ -621,7 +711,7 @@ def run_profile_batch(scale=4, launches=3):
     rng = np.random.default_rng(SEED)
     plans, xs, ys = [], [], []
     for q, n, cnt, g in SEGMENTS:
-        plans.append(gb.Plan(gb.Kind.R4_I16_FWD, n, q, root_of(q, n, g)))
+        plans.append(gb.Plan(gb.Kind.R4_I16_FWD, n, q, root_of(q, n, g), 0, flags))
         xs.append(torch.from_numpy(rng.integers(0, q, (cnt * scale, n)).astype(np.int16)).cuda())
         ys.append(torch.empty_like(xs[-1]))
     batch = gb.Batch(list(zip(plans, xs, ys)))
@@ -636,7 +726,8 @@ def run_profile_batch(scale=4, launches=3):
     batch.status()
     ms = a.elapsed_time(b)
     nbytes = sum(2 * x.numel() * 2 for x in xs)
-    print(json.dumps({"case": f"batch_x{scale}", "polys": sum(x.shape[0] for x in xs), "ms": ms,
+    print(json.dumps({"case": f"batch_x{scale}", "flags": flags, "el": batch.query(4), "cta_per_sm_cfg": None,
+                      "polys": sum(x.shape[0] for x in xs), "ms": ms,
                       "algorithmic_GBps": nbytes / (ms / 1e3) / 1e9}))
 
 
@@ -647,6 +738,8 @@ def run_profile_case(name, launches=3):
     import ntts_on_amd_ai_engines_aie1_gb300 as gb
     if name == "batch_r4":
         return run_profile_batch(4, launches)
+    if name == "c_batch_r4":
+        return run_profile_batch(4, launches, flags=1)
     kind, n, q, root, polys, *fl = PROFILE_CASES[name]
     plan = gb.Plan(kind, n, q, root, 0, fl[0] if fl else 0)
     dt = torch.int32 if plan.elem_bytes == 4 else torch.int16
@@ -673,6 +766,9 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--arith", choices=["canonical", "lanes"], default="canonical",
+                    help="outputs of the timed workload: canonical residues (default) or the reference's "
+                         "partially reduced lanes")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-per-ntt", action="store_true")

@@ -120,10 +120,19 @@ int gbntt_plan_destroy(gbntt_plan* plan);
 /* Transforms `batch` polynomials held in device memory, asynchronously on
  * `stream` (a cudaStream_t; NULL = legacy default stream).  One kernel launch
  * per call, except the int32 designs with n >= 2^16 (up to 2^22), which run
- * two passes (column and row sub-transforms) per chunk of at most 64 MiB of
- * polynomials. */
+ * two passes (column and row sub-transforms) per chunk of polynomials (at most
+ * 64 MiB; 48 MiB for the canonical four-step, whose column pass moves 2D tiles
+ * with the Tensor Memory Accelerator and whose row pass applies the four-step
+ * twist).  The environment variable GBNTT_FOURSTEP_MIN_L (14, 15 or 16, read
+ * once per process) moves the canonical int32 plans of n >= 2^that length to
+ * the four-step (default 16: n = 2^14 and 2^15 run one CTA per polynomial). */
 int gbntt_execute(const gbntt_plan* plan, const void* d_in, void* d_out, uint64_t batch,
                   void* stream);
+
+/* Synchronous: GBNTT_ERR_TIMEOUT if a bounded wait in an earlier launch of
+ * this plan ran out (the TMA tile loads of the canonical int32 four-step,
+ * n >= 2^16; the other designs have no waits); the call clears it. */
+int gbntt_plan_status(const gbntt_plan* plan);
 
 /* Same, on host buffers, and waits for the stream; serialised per plan.  When
  * both buffers are page-locked and mapped into the device's address space

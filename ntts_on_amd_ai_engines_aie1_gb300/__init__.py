@@ -111,6 +111,7 @@ def lib():
         L.gbntt_server_submit_schedule.argtypes = [vp, u64, ctypes.POINTER(u32), ctypes.POINTER(vp),
                                                    ctypes.POINTER(vp), ctypes.POINTER(u64),
                                                    ctypes.POINTER(ctypes.c_double), ctypes.POINTER(u64)]
+        L.gbntt_plan_status.argtypes = [vp]
         L.gbntt_batch_execute_noalloc.argtypes = [ctypes.POINTER(Segment), u32, vp]
         L.gbntt_noalloc_status.argtypes = []
         L.gbntt_set_wait_limit.argtypes = [u32]
@@ -218,6 +219,11 @@ class Plan:
             out = torch.empty_like(x)
         self.execute(x, out, x.numel() // self.n, stream)
         return out
+
+    def status(self):
+        """Raises NTTError (GBNTT_ERR_TIMEOUT) if a bounded wait in an earlier
+        launch of this plan ran out; clears it."""
+        _check(lib().gbntt_plan_status(self.handle))
 
     def execute_host(self, h_in, h_out, batch=None, stream=None):
         """Host buffers (numpy arrays or torch CPU tensors); synchronous."""

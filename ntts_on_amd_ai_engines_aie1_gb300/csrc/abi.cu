@@ -2,12 +2,14 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
 #include <string>
 
 #include "../../include/gb300_ntt.h"
+#include "batch_kernel.cuh"
 #include "canon_tables.h"
 #include "device.cuh"
 #include "plan_internal.h"
@@ -26,6 +28,10 @@ struct gbntt_plan {
     KernelInfo ki;
     KernelInfo kl;         // latency form for launches of at most one CTA per SM (fn nullptr: none)
     LargeInfo large;       // int32 n >= 2^16: two-pass schedule (large.cols != nullptr)
+    CanonLarge clarge;     // canonical int32 n >= 2^16: four-step (clarge.cols != nullptr)
+    const int2* tab_rows = nullptr;   // four-step: the row transforms' table (inside d_tab)
+    const int2* twist = nullptr;      // four-step: twist factors (inside d_tab)
+    unsigned* d_err = nullptr;        // four-step: set when a bounded wait ran out
     KArgs base;            // constants shared by every launch
     int2* d_tab = nullptr;
     size_t tab_bytes = 0;
@@ -77,13 +83,33 @@ KernelInfo kernel_for(int fam, int L, bool br, bool lat) {
     }
 }
 
+// Canonical int32 lengths from 2^L on run as the four-step (two passes);
+// shorter ones (up to 2^15) in one CTA per polynomial.  GBNTT_FOURSTEP_MIN_L
+// (14 .. 16) overrides the default, read once per process.
+int fourstep_min_L() {
+    static const int v = [] {
+        const char* e = std::getenv("GBNTT_FOURSTEP_MIN_L");
+        const int x = e ? std::atoi(e) : 16;
+        return x >= 14 && x <= 16 ? x : 16;
+    }();
+    return v;
+}
+
 int launch(const gbntt_plan* p, const void* d_in, void* d_out, uint64_t batch, cudaStream_t s) {
     KArgs a = p->base;
     a.in = d_in;
     a.out = d_out;
     a.batch = (long long)batch;
     cudaError_t e = cudaSuccess;
-    if (p->large.cols) {
+    if (p->clarge.cols) {
+        const bool inverse = (p->hp.kind == K_R2_I32_INV);
+        int nl = 0;
+        e = launch_canon_large(p->clarge, a, p->d_tab, p->tab_rows, p->twist, d_in, d_out, (long long)batch, inverse,
+                               p->d_err, s, &nl);
+        if (e != cudaSuccess) return cuda_fail(e, "four-step launch");
+        g_launches.fetch_add((unsigned long long)nl, std::memory_order_relaxed);
+        return GBNTT_OK;
+    } else if (p->large.cols) {
         // two passes per chunk of polynomials; a chunk (<= 64 MiB) stays in L2
         // between its passes.  Forward: columns then rows; inverse: rows first.
         const LargeInfo& li = p->large;
@@ -240,10 +266,17 @@ int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t
     // GBNTT_FLAG_CANONICAL without GBNTT_FLAG_LANE_EXACT: the canonical family
     // of the design's direction and storage type (the two-pass int32 lengths
     // keep the reference's lane arithmetic plus the final reduction)
-    const bool canon = canonical_fast(kind, hp.q, flags) && hp.L < 16;
+    const bool canon = canonical_fast(kind, hp.q, flags);
     p->fam = canon ? canonical_family(kind) : family_of(kind);
     p->br = !canon && (kind == K_R4_I16_INV);
-    if (p->fam >= 0 && hp.L >= 16) {
+    if (canon && hp.elem_bytes == 4 && hp.L >= fourstep_min_L() &&
+        (hp.L >= 16 || !(flags & FLAG_NATURAL_ORDER))) {   // the four-step has no natural-order form
+        p->clarge = canon_large_info(p->fam, hp.L);
+        if (!p->clarge.cols) {
+            delete p;
+            return fail(GBNTT_ERR_LENGTH, "no kernel for this length");
+        }
+    } else if (p->fam >= 0 && hp.L >= 16) {
         p->large = large_info(p->fam, hp.L);
         if (!p->large.cols) {
             delete p;
@@ -269,6 +302,14 @@ int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t
             return cuda_fail(e, "cudaFuncSetAttribute");
         }
     }
+    if (p->clarge.cols) {
+        e = raise_smem_limit(p->clarge.cols, p->clarge.cols_smem);
+        if (e == cudaSuccess) e = raise_smem_limit(p->clarge.rows, p->clarge.rows_smem);
+        if (e != cudaSuccess) {
+            delete p;
+            return cuda_fail(e, "cudaFuncSetAttribute");
+        }
+    }
     if (p->large.cols) {
         e = cudaFuncSetAttribute(p->large.cols, cudaFuncAttributeMaxDynamicSharedMemorySize, p->large.cols_smem);
         if (e == cudaSuccess)
@@ -279,8 +320,7 @@ int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t
         }
     }
     if (kind == K_BITREV_I16 && bitrev_smem_bytes(hp.L) > 48 * 1024) {
-        e = cudaFuncSetAttribute(bitrev_kernel_ptr(), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 bitrev_smem_bytes(hp.L));
+        e = raise_smem_limit(bitrev_kernel_ptr(), bitrev_smem_bytes(hp.L));
         if (e != cudaSuccess) {
             delete p;
             return cuda_fail(e, "cudaFuncSetAttribute");
@@ -291,18 +331,44 @@ int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t
     const bool inverse = (kind == K_R2_I16_INV || kind == K_R2_I32_INV || kind == K_R4_I16_INV);
     std::vector<int32_t> dev_tab;
     if (canon) {
-        // canonical families: (w, w') pairs computed on the device
-        p->tab_bytes = canon_table_entries(hp.L, inverse) * sizeof(int2);
+        // canonical families: (w, w') pairs computed on the device; the
+        // four-step holds the column and row transforms' tables and the twist
+        const CanonLarge& cl = p->clarge;
+        size_t n_cols = canon_table_entries(hp.L, inverse), n_rows = 0, n_twist = 0;
+        if (cl.cols) {
+            n_cols = canon_table_entries(cl.L1, inverse);
+            n_rows = canon_table_entries(cl.L2, inverse);
+            n_twist = canon_twist_entries(cl.L1, cl.L2, cl.row_el);
+        }
+        p->tab_bytes = (n_cols + n_rows + n_twist) * sizeof(int2);
         e = cudaMalloc(&p->d_tab, p->tab_bytes);
+        if (e == cudaSuccess && cl.cols) e = cudaMalloc(&p->d_err, 256);
         if (e != cudaSuccess) {
+            if (p->d_tab) cudaFree(p->d_tab);
             delete p;
             return e == cudaErrorMemoryAllocation ? fail(GBNTT_ERR_NOMEM, "device allocation failed")
                                                   : cuda_fail(e, "cudaMalloc");
         }
-        e = make_canon_table(p->d_tab, hp.L, (uint32_t)hp.q, (uint32_t)hp.root, inverse, 0);
+        const uint32_t q32 = (uint32_t)hp.q;
+        if (cl.cols) {
+            const int64_t n1 = (int64_t)1 << cl.L1, n2 = (int64_t)1 << cl.L2;
+            p->tab_rows = p->d_tab + n_cols;
+            p->twist = p->d_tab + n_cols + n_rows;
+            e = make_canon_table(p->d_tab, cl.L1, q32, (uint32_t)powmod(hp.root, (uint64_t)n2, hp.q), inverse, 0);
+            if (e == cudaSuccess)
+                e = make_canon_table(p->d_tab + n_cols, cl.L2, q32, (uint32_t)powmod(hp.root, (uint64_t)n1, hp.q),
+                                     inverse, 0);
+            if (e == cudaSuccess)
+                e = make_canon_twist(p->d_tab + n_cols + n_rows, cl.L1, cl.L2, cl.row_el, q32, (uint32_t)hp.root,
+                                     inverse, 0);
+            if (e == cudaSuccess) e = cudaMemsetAsync(p->d_err, 0, 256, 0);
+        } else {
+            e = make_canon_table(p->d_tab, hp.L, q32, (uint32_t)hp.root, inverse, 0);
+        }
         if (e == cudaSuccess) e = cudaStreamSynchronize(0);
         if (e != cudaSuccess) {
             cudaFree(p->d_tab);
+            if (p->d_err) cudaFree(p->d_err);
             delete p;
             return cuda_fail(e, "canonical table");
         }
@@ -371,10 +437,23 @@ int gbntt_plan_create(gbntt_plan** out, int kind, uint32_t n, int64_t q, int64_t
 int gbntt_plan_destroy(gbntt_plan* p) {
     if (!p) return GBNTT_OK;
     if (p->d_tab) cudaFree(p->d_tab);
+    if (p->d_err) cudaFree(p->d_err);
     if (p->d_stage) cudaFree(p->d_stage);
     if (p->zc_state) gbntt_internal_zc_free(p->zc_state);
     delete p;
     return GBNTT_OK;
+}
+
+int gbntt_plan_status(const gbntt_plan* p) {
+    if (!p) return fail(GBNTT_ERR_ARG, "plan is null");
+    if (!p->d_err) return GBNTT_OK;
+    unsigned w = 0;
+    cudaError_t e = cudaMemcpy(&w, p->d_err, sizeof(w), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "status read");
+    if (!w) return GBNTT_OK;
+    e = cudaMemset(p->d_err, 0, sizeof(w));
+    if (e != cudaSuccess) return cuda_fail(e, "status reset");
+    return fail(GBNTT_ERR_TIMEOUT, "a tile load of the four-step column pass did not arrive within the wait limit");
 }
 
 int gbntt_plan_query(const gbntt_plan* p, int what, int64_t* value) {

@@ -59,7 +59,12 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
     KArgs* ka = reinterpret_cast<KArgs*>(bsmem + 64);
     unsigned char* stage0 = bsmem + SMEM_HEADER;
     int* xbuf = reinterpret_cast<int*>(bsmem + SMEM_HEADER + 2 * stage_bytes);
-    __shared__ long long sh_next;
+    // sh_next[i]: the tile after the one in buffer i.  Thread 0 writes slot
+    // buf at the top of an iteration and every thread reads it after the
+    // iteration's last barrier; the next write to that slot comes two
+    // iterations later, after the next iteration's last barrier, so no thread
+    // can read a value from the wrong iteration.
+    __shared__ long long sh_next[2];
     __shared__ int sh_pending[2];
     __shared__ int sh_failed;
     const int tid = threadIdx.x;
@@ -90,7 +95,7 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
         mbar_init(&bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         const long long t0 = (long long)atomicAdd(&b.ctr[CTR_NEXT], 1ull);
-        sh_next = t0;
+        sh_next[1] = t0;
         sh_pending[0] = 0;
         sh_pending[1] = 0;
         sh_failed = 0;
@@ -100,7 +105,7 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
         }
     }
     __syncthreads();
-    long long t = sh_next;
+    long long t = sh_next[1];
     unsigned phases = 0u;    // bit i: parity of the next completion of bar[i]
     int buf = 0;
     int cur_seg = -1;
@@ -110,7 +115,7 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
         const SegDev* sd = &b.segs[s];
         if (tid == 0) {
             const long long tn = (long long)atomicAdd(&b.ctr[CTR_NEXT], 1ull);
-            sh_next = tn;
+            sh_next[buf] = tn;
             if (tn < total) {
                 bulk_wait_read();           // the other buffer's last store has left shared memory
                 issue(tn, buf ^ 1, s);
@@ -144,7 +149,7 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
             default: break;
         }
         __syncthreads();
-        const long long tnext = sh_next;
+        const long long tnext = sh_next[buf];
         if (sh_failed) break;
         if (tid == 0) {
             sh_pending[buf] = 0;

@@ -29,22 +29,17 @@ __device__ __forceinline__ int2 shoup_pair(unsigned w, unsigned q) {
     return make_int2((int)w, (int)(unsigned)(((unsigned long long)w << 32) / q));
 }
 
-// forward (n/2 entries): entry b = root^bitrev_{L-1}(b), the twiddle of block b
-// in every layer.  inverse (n entries): entry 2^B + j = root^(-j 2^(L-1-B)),
-// the twiddle of the layer on bit B at low position bits j; entry 0 = 1.
+// n entries: entry 2^B + j = root^(+-j 2^(L-1-B)) (+ forward, - inverse), the
+// twiddle of the layer on bit B at low position bits j; entry 0 = 1.
 __global__ void k_canon_table(int2* tab, int L, unsigned q, unsigned root, int inverse) {
     const int n = 1 << L;
-    const int count = inverse ? n : n / 2;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        unsigned long long e;
-        if (!inverse) {
-            e = L > 1 ? (__brev((unsigned)i) >> (33 - L)) : 0;
-        } else if (i == 0) {
-            e = 0;
-        } else {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        unsigned long long e = 0;
+        if (i > 0) {
             const int B = 31 - __clz(i);
             const unsigned long long j = (unsigned long long)(i - (1 << B));
-            e = (unsigned long long)n - ((j << (L - 1 - B)) & (unsigned long long)(n - 1));
+            e = (j << (L - 1 - B)) & (unsigned long long)(n - 1);
+            if (inverse && e) e = (unsigned long long)n - e;
         }
         tab[i] = shoup_pair(powmod_dev(root, e, q), q);
     }
@@ -82,7 +77,7 @@ int grid_of(long long count) {
 
 }  // namespace
 
-size_t canon_table_entries(int L, bool inverse) { return inverse ? (size_t)1 << L : (size_t)1 << (L - 1); }
+size_t canon_table_entries(int L, bool) { return (size_t)1 << L; }
 
 cudaError_t make_canon_table(int2* d_tab, int L, uint32_t q, uint32_t root, bool inverse, cudaStream_t s) {
     k_canon_table<<<grid_of((long long)canon_table_entries(L, inverse)), 256, 0, s>>>(d_tab, L, q, root,

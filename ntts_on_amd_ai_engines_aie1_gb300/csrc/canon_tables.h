@@ -8,7 +8,7 @@
 
 namespace gbntt {
 
-// (w, floor(w 2^32 / q)) pairs: forward n/2 entries, inverse n entries
+// (w, floor(w 2^32 / q)) pairs, n entries: root^(+-j 2^(L-1-B)) at 2^B + j
 size_t canon_table_entries(int L, bool inverse);
 cudaError_t make_canon_table(int2* d_tab, int L, uint32_t q, uint32_t root, bool inverse, cudaStream_t s);
 

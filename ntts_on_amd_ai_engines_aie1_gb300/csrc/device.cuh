@@ -186,13 +186,19 @@ __host__ __device__ __forceinline__ int canon(int x, int q, int c) {
 //     2014): for a twiddle w < q with w' = floor(w 2^32 / q) and any y < 2^32,
 //     y w - floor(y w' / 2^32) q lies in [0, 2q); the low 32 bits of the two
 //     products give it exactly (mul.hi + two IMADs);
-//   * a Cooley-Tukey butterfly x +- t (t the Shoup product) leaves x + t and
-//     x - t + 2q, so the bound on the lanes grows by 2q per layer.  int16
-//     moduli (q < 2^15) start below 2^18 and never come near 2^32 in 12
-//     layers: no correction at all.  int32 moduli (q < 2^30) keep the Harvey
-//     bound: x is brought from [0, 4q) to [0, 2q) before each butterfly
-//     (one subtraction and an unsigned minimum), outputs stay below 4q;
+//   * the inverse runs Cooley-Tukey butterflies: x +- t (t the Shoup product)
+//     leaves x + t and x - t + 2q, so the bound on the lanes grows by 2q per
+//     layer.  int16 moduli (q < 2^15) start below 2^18 and stay below 2^20
+//     in 12 layers: no correction at all.  int32 moduli (q < 2^30) keep
+//     Harvey's bound: x is brought from [0, 4q) to [0, 2q) before each
+//     butterfly (one subtraction and an unsigned minimum), outputs below 4q;
+//   * the forward runs Gentleman-Sande butterflies: x + y and (x - y + c) w
+//     with c a multiple of q above y's bound.  int16 sums double the bound
+//     each layer and stay below 2^29 in 12 layers; int32 sums are folded
+//     back below 2q, so every lane stays in [0, 2q);
 //   * one reduction to [0, q) at the end.
+// Both cost three multiplies and two (int16) or four (int32) additions,
+// subtractions and minimums per butterfly.
 // ---------------------------------------------------------------------------
 
 __device__ __forceinline__ unsigned shoup_mul(unsigned y, unsigned w, unsigned wq, unsigned q) {
@@ -578,37 +584,64 @@ __device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const
     for (int r = 0; r < (E >> W); ++r) {
         const int k0 = ((r >> KB) << (KB + W)) | (r & ((1 << KB) - 1));
         if constexpr (fam_canon(FAM)) {
-            // canonical Cooley-Tukey butterfly (x, y) -> (x + w y, x - w y).
-            // Forward: layer S pairs the positions differing in bit B = L-1-S,
-            // w = root^bitrev_{L-1}(block), block = the position bits above B
-            // (one table of n/2 entries serves every layer).  Inverse on
-            // bit-reversed input: bit B = S, w = root^(-j 2^(L-1-B)) with
-            // j = the position bits below B, at table entry 2^B + j.
-            static_assert(!HIB && XC == 0, "the canonical families run whole sub-transforms");
+            // Canonical butterflies.  Both directions index the table by the
+            // position bits below the butterfly bit B, j = pos mod 2^B, at entry
+            // 2^B + j, so a warp's twiddle loads are one broadcast (j from the
+            // registers) or consecutive entries (j from the lane index).
+            static_assert(!HIB, "the canonical families run whole sub-transforms (the four-step twist is separate)");
             const int k1 = k0 | (1 << KB);
             const unsigned uq = (unsigned)q, q2 = uq << 1;
-            if constexpr (S == 0) {
-                // the first layer has the twiddle 1 everywhere (block 0 of
-                // the forward transform, span 1 of the inverse one)
+            if constexpr (topdown(FAM)) {
+                // Forward: Gentleman-Sande, natural order in, bit-reversed out.
+                // Layer S pairs the positions differing in bit B = L-1-S:
+                // (x, y) -> (x + y, (x - y) w), w = root^(j 2^(L-1-B)).  The
+                // last layer (B = 0) has w = 1.
+                const unsigned x = (unsigned)v[k0], y = (unsigned)v[k1];
+                unsigned s, d;
+                if constexpr (fam_i32(FAM)) {
+                    // lanes in [0, 2q): the sum is folded back below 2q
+                    s = x + y;
+                    d = x + q2 - y;
+                    if constexpr (S != L - 1) s = lazy_sub(s, q2);
+                } else if constexpr (S == 0) {
+                    // raw int16 inputs in [-2^15, 2^15): 2M (a multiple of q,
+                    // M >= 2^15) makes both lanes non-negative, below 2^18
+                    s = (unsigned)((int)x + (int)y + a.in_off);
+                    d = (unsigned)((int)x - (int)y + a.in_off);
+                } else {
+                    // int16 lanes below 2^(S+1) 2M: sums double the bound each
+                    // layer (below 2^29 after 12 layers); the difference takes
+                    // the offset 2^S 2M, a multiple of q above the bound
+                    s = x + y;
+                    d = x + ((unsigned)a.in_off << S) - y;
+                }
+                if constexpr (S != L - 1) {
+                    const int2 t = __ldg(&a.tab[(1 << B) + (posmap<LO, EL>(g, k0) & ((1 << B) - 1))]);
+                    d = shoup_mul(d, (unsigned)t.x, (unsigned)t.y, uq);
+                }
+                v[k0] = (int)s;
+                v[k1] = (int)d;
+            } else if constexpr (S == 0) {
+                // Inverse: Cooley-Tukey on bit-reversed input, natural order
+                // out.  Layer S pairs the positions differing in bit B = S:
+                // (x, y) -> (x + w y, x - w y), w = root^(-j 2^(L-1-B)); the
+                // first layer (span 1) has w = 1.
                 if constexpr (fam_i32(FAM)) {
                     // lanes in [0, 2q) from the prologue
                     const unsigned x = (unsigned)v[k0], y = (unsigned)v[k1];
                     v[k0] = (int)(x + y);
                     v[k1] = (int)(x + q2 - y);
                 } else {
-                    // raw int16 inputs in [-2^15, 2^15): adding 2M (a multiple
-                    // of q, M >= 2^15) makes both lanes non-negative, below 2^18
+                    // raw int16 inputs: the offset 2M as in the forward
                     const int x = v[k0], y = v[k1];
                     v[k0] = x + y + a.in_off;
                     v[k1] = x - y + a.in_off;
                 }
             } else {
-                int2 t;
-                if constexpr (topdown(FAM)) {
-                    t = __ldg(&a.tab[posmap<LO, EL>(g, k0) >> (B + 1)]);
-                } else {
-                    t = __ldg(&a.tab[(1 << B) + (posmap<LO, EL>(g, k0) & ((1 << B) - 1))]);
-                }
+                // the lane bound grows by 2q per layer (int16: below 2^20 after
+                // 12 layers); int32 lanes keep Harvey's bound, x < 2q before the
+                // butterfly and both outputs below 4q
+                const int2 t = __ldg(&a.tab[(1 << B) + (posmap<LO, EL>(g, k0) & ((1 << B) - 1))]);
                 unsigned x = (unsigned)v[k0];
                 if constexpr (fam_i32(FAM)) x = lazy_sub(x, q2);
                 const unsigned m = shoup_mul((unsigned)v[k1], (unsigned)t.x, (unsigned)t.y, uq);
@@ -1019,6 +1052,26 @@ struct LargeInfo {
     int L1 = 0, L2 = 0;           // high (column-pass) and low (row-pass) index bits
 };
 LargeInfo large_info(int fam, int L);
+
+// Canonical int32 transforms of 2^14 .. 2^22 coefficients as a four-step
+// (kernels_c32_large.cu): n = n1 n2, rows of n2 coefficients.  Forward:
+// column transforms (length n1, root^n2, bit-reversed along the column), the
+// twist root^(c bitrev(r)) of row r at column c, row transforms (length n2,
+// root^n1, bit-reversed along the row).  Inverse: the same steps reversed.
+struct CanonLarge {
+    const void* cols = nullptr;   // k_ccols: TMA-tiled column pass
+    const void* rows = nullptr;   // k_crows: row pass with the twist
+    int cols_threads = 0, cols_smem = 0, cols_width = 0;   // columns per CTA
+    int rows_threads = 0, rows_smem = 0, rows_per_cta = 0;
+    int L1 = 0, L2 = 0, row_el = 0;
+};
+CanonLarge canon_large_info(int fam, int L);
+// the four-step launches of one call: `in` -> `out` (in place allowed);
+// tab_cols/tab_rows: the sub-transforms' tables, twist: the factors;
+// err: a device word set when a bounded wait runs out
+cudaError_t launch_canon_large(const CanonLarge& li, const KArgs& base, const int2* tab_cols, const int2* tab_rows,
+                               const int2* twist, const void* in, void* out, long long batch, bool inverse,
+                               unsigned* err, cudaStream_t s, int* launches);
 
 // single-purpose kernels (kernels_misc.cu)
 cudaError_t launch_r8_stage(const KArgs& a, int L, cudaStream_t s);

@@ -112,9 +112,16 @@ __global__ void __launch_bounds__(256) k_full_barrett(const KArgs a, long long t
         out[j] = (short)fb16(in[j], fs, wq, a.q);
 }
 
+// grid of a grid-stride kernel: enough CTAs for the work, at most 16 per SM
 int grid_for(long long work, int threads) {
+    static const int sms = [] {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        return n > 0 ? n : 1;
+    }();
     long long b = (work + threads - 1) / threads;
-    const long long cap = 152LL * 16;
+    const long long cap = (long long)sms * 16;
     if (b > cap) b = cap;
     return b < 1 ? 1 : (int)b;
 }

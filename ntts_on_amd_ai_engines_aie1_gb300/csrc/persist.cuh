@@ -129,6 +129,33 @@ __device__ __forceinline__ void stage_read(int (&v)[1 << EL], const void* stage,
     }
 }
 
+// reads one staged polynomial in the window at bit 0: thread g's contiguous
+// run of E coefficients, with 16-byte accesses
+template <bool I32, int L, int EL>
+__device__ __forceinline__ void stage_read_run(int (&v)[1 << EL], const void* stage, int lp, int g) {
+    constexpr int E = 1 << EL, N = 1 << L;
+    if constexpr (I32) {
+        const int4* s4 = reinterpret_cast<const int4*>(static_cast<const int*>(stage) + lp * N + g * E);
+#pragma unroll
+        for (int j = 0; j < E / 4; ++j) {
+            const int4 w = s4[j];
+            v[4 * j] = w.x; v[4 * j + 1] = w.y; v[4 * j + 2] = w.z; v[4 * j + 3] = w.w;
+        }
+    } else {
+        const int4* s4 = reinterpret_cast<const int4*>(static_cast<const short*>(stage) + lp * N + g * E);
+#pragma unroll
+        for (int j = 0; j < E / 8; ++j) {
+            const int4 w = s4[j];
+            const int ww[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                v[8 * j + 2 * h] = (int)(short)(ww[h] & 0xFFFF);
+                v[8 * j + 2 * h + 1] = ww[h] >> 16;
+            }
+        }
+    }
+}
+
 // ka: the segment's arguments in shared memory, read only where the output
 // options are applied (natural order, n^-1 scaling, canonical form)
 template <int FAM, int L, int CTA, int ELMAX>
@@ -147,11 +174,22 @@ __device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KC&
     const bool active = lp < npolys;
     int* sp = xbuf + lp * SW;
     int v[E];
+    // A first window on the low bits (the inverse designs) reads each thread's
+    // contiguous run with 16-byte accesses, unless the input is in natural
+    // order; otherwise the strided read, then an exchange to the first window.
+    constexpr bool RUN_READ = LO0 == 0 && LO0 != LOS && (I32 ? E >= 4 : E >= 8);
+    bool in_window = false;
     if (active) {
         // natural-order input of an inverse design: the bit reversal is the read pattern
         if constexpr (fam_natural_in(FAM, false)) {
-            if (ka.natural_in) stage_read<I32, L, EL, LOS, true>(v, stage, lp, g);
-            else stage_read<I32, L, EL, LOS, false>(v, stage, lp, g);
+            if (ka.natural_in) {
+                stage_read<I32, L, EL, LOS, true>(v, stage, lp, g);
+            } else if constexpr (RUN_READ) {
+                stage_read_run<I32, L, EL>(v, stage, lp, g);
+                in_window = true;
+            } else {
+                stage_read<I32, L, EL, LOS, false>(v, stage, lp, g);
+            }
         } else {
             stage_read<I32, L, EL, LOS, false>(v, stage, lp, g);
         }
@@ -160,7 +198,15 @@ __device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KC&
         for (int k = 0; k < E; ++k) v[k] = 0;
     }
     prologue<FAM>(v, ka);
-    if constexpr (LO0 != LOS) exchange_windows<L, EL, LOS, LO0>(v, sp, g);
+    if constexpr (LO0 != LOS) {
+        // the CTA agrees on the path (natural_in is the segment's): every
+        // thread takes the exchange or none does
+        if constexpr (RUN_READ) {
+            if (!__syncthreads_or(in_window)) exchange_windows<L, EL, LOS, LO0>(v, sp, g);
+        } else {
+            exchange_windows<L, EL, LOS, LO0>(v, sp, g);
+        }
+    }
     run_steps<FAM, L, EL>(v, sp, g, a, std::make_integer_sequence<int, NS>{});
     epilogue<FAM, false>(v, ka);
     if (!active) return;

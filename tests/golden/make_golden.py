@@ -1,6 +1,7 @@
 """Regenerates tests/golden/ref_tables.json from the reference's own table code.
 
-Run in a checkout that has the reference sources (default /root/reference):
+Run where the reference sources are (argument, else $GBNTT_REFERENCE_ROOT,
+else `reference` beside this repository):
 
     python tests/golden/make_golden.py [REF_DIR]
 
@@ -18,6 +19,11 @@ import os
 import subprocess
 import sys
 
+
+def default_reference_root():
+    repo = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    return os.environ.get("GBNTT_REFERENCE_ROOT") or os.path.join(os.path.dirname(repo), "reference")
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 
@@ -27,7 +33,7 @@ def table_hash(values):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else default_reference_root()
     oracle = os.path.join(ROOT, "oracle")
     subprocess.run(["make", "-s", "-C", oracle, "ref", f"REF={ref}"], check=True)
     out = subprocess.run([os.path.join(oracle, "_ref", "ref_tables")], check=True,

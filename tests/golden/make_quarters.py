@@ -7,10 +7,17 @@ of each stream (n = 4096 for the int16 designs, 2048 for the int32 designs,
 the lengths of src/project.cpp:139-157) under tests/golden/quarters/, so the
 tests can run the harness format without the reference tree.
 
-    python tests/golden/make_quarters.py [reference root, default /root/reference]
+    python tests/golden/make_quarters.py [reference root]
+
+(default: $GBNTT_REFERENCE_ROOT, else `reference` beside this repository)
 """
 import os
 import sys
+
+
+def default_reference_root():
+    repo = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    return os.environ.get("GBNTT_REFERENCE_ROOT") or os.path.join(os.path.dirname(repo), "reference")
 
 POLYS = 4
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -31,4 +38,4 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else default_reference_root())

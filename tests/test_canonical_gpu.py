@@ -198,3 +198,39 @@ def test_lane_exact_reproduces_the_reference_wrap(gb, orc):
     fast = gpu_run(gb, 1, n, q, root, x, flags=gb.FLAG_CANONICAL)
     assert np.array_equal(lane.astype(np.int64), ref)
     assert np.array_equal(fast.astype(np.int64), exact)
+
+
+@pytest.mark.parametrize("L", [16, 17, 18, 19, 20, 21, 22])
+@pytest.mark.parametrize("q", [998244353, 754974721])
+def test_canonical_int32_four_step(gb, orc, q, L):
+    """n = 2^16 .. 2^22: TMA-tiled column pass, twist, row pass; against the
+    exact transform, both directions, out of place and in place, with the
+    fused n^-1 on the inverse, and the round trip."""
+    n = 1 << L
+    rng = np.random.default_rng(SEED + 3900 + L)
+    batch = 1 if L >= 21 else 3 if L >= 19 else 5
+    root = root_for(q, n)
+    x = inputs(rng, batch, n, -(1 << 31), 1 << 31, np.int32)
+    y = gpu_run(gb, 4, n, q, root, x, flags=gb.FLAG_CANONICAL)
+    assert np.array_equal(y.astype(np.int64), orc.ntt_exact(x, q, root))
+    z = gpu_run(gb, 5, n, q, root, y, flags=gb.FLAG_CANONICAL, inplace=True)
+    assert np.array_equal(z.astype(np.int64), (x.astype(np.int64) % q) * n % q)
+    w = gpu_run(gb, 5, n, q, root, x, flags=gb.FLAG_CANONICAL | gb.FLAG_SCALE_NINV)
+    assert np.array_equal(w.astype(np.int64), orc.ntt_exact(x, q, root, inverse=True) * pow(n, -1, q) % q)
+    yi = gpu_run(gb, 4, n, q, root, x, flags=gb.FLAG_CANONICAL, inplace=True)
+    assert np.array_equal(yi, y)
+
+
+def test_canonical_four_step_status_and_many_chunks(gb, orc):
+    """A batch spanning several L2 chunks (48 MiB each) and the plan's status call."""
+    q, n = 469762049, 1 << 20
+    root = root_for(q, n)
+    x = np.random.default_rng(SEED + 3990).integers(0, q, (26, n)).astype(np.int32)
+    plan = gb.Plan(4, n, q, root, 0, gb.FLAG_CANONICAL)
+    t = torch.from_numpy(x).cuda()
+    y = plan(t)
+    torch.cuda.synchronize()
+    plan.status()
+    got = y.cpu().numpy()
+    for i in (0, 11, 12, 25):
+        assert np.array_equal(got[i].astype(np.int64), orc.ntt_exact(x[i:i + 1], q, root)[0])
