@@ -61,10 +61,8 @@ def coeffs_per_poly():
 def oracle_outputs(oracle, x, q, n, g, arith, threads=1):
     """The reference's algorithm (the oracle's restatement) on x; reduced mod q
     for canonical outputs."""
-    y = oracle.Plan(oracle.R4_I16_FWD, n, q, root_of(q, n, g))(x, threads=threads)
-    if arith == "canonical":
-        y = np.mod(y, q, dtype=np.int16) if y.dtype == np.int16 else np.mod(y, q)
-    return y
+    return oracle.Plan(oracle.R4_I16_FWD, n, q, root_of(q, n, g))(x, threads=threads,
+                                                                   canonical=arith == "canonical")
 
 
 def max_over_ranks(x, dist=None, device="cpu"):
@@ -229,7 +227,7 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": "NTT/s", "cores": threads, "kind": "port",
                          "sample": desc + "; the reference's AIE kernels cannot be built here, so its CPU "
                                           "restatement (oracle/ntt_oracle.c, the parity oracle) is timed"
-                                          + ("; outputs reduced mod q" if args.arith == "canonical" else "")},
+                                          + ("; outputs reduced mod q in the same threads" if args.arith == "canonical" else "")},
         "e2e": {"value": value, "unit": "NTT/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -356,7 +354,7 @@ def run_ours(args):
 
     serving = None
     if rank == 0 and not args.skip_serve:
-        serving = run_serving(gb, args.serve_seconds)
+        serving = run_serving(gb, args.serve_seconds, args.arith)
 
     if rank != 0:
         if dist:
@@ -369,7 +367,7 @@ def run_ours(args):
         cpu = {"value": v, "unit": "NTT/s", "cores": threads, "kind": "port",
                "sample": f"{done} NTTs of the same workload in {el:.1f} s (whole batches), oracle/ntt_oracle.c "
                          f"with {threads} threads; the reference's AIE kernels cannot be built here"
-                         + ("; outputs reduced mod q" if args.arith == "canonical" else "")}
+                         + ("; outputs reduced mod q in the same threads" if args.arith == "canonical" else "")}
     tr = (traffic or {}).get("headline_" + args.arith) or {}
     line = {
         "metric": METRIC, "value": value, "unit": "NTT/s", "n_gpus": world, "steps": args.steps,
@@ -378,7 +376,8 @@ def run_ours(args):
         "config": workload_config(args.arith, world),
         "coefficients_per_s": value * coeffs_per_poly(),
         "run": {"launch": "one persistent kernel, CUDA graph replay", "arithmetic": args.arith,
-                "autotuned_log2_coeffs_per_thread": batch.query(4), "autotuned_cta_threads": batch.query(6)},
+                "autotuned_log2_coeffs_per_thread": batch.query(4), "autotuned_cta_threads": batch.query(6),
+                "autotuned_ctas_per_sm_budget": batch.query(7)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src,
                      "kernel": f"k_batch<int16> persistent radix-4 ({args.arith} arithmetic, all 16384 polys "
@@ -578,7 +577,7 @@ def run_configs(gb, oracle, flush, stream, peak, arith):
 SERVE_Q32 = [(998244353, 3), (469762049, 3), (167772161, 3), (754974721, 11)]   # (q, generator)
 
 
-def run_serving(gb, seconds):
+def run_serving(gb, seconds, arith="canonical"):
     """Serving loop over a stream of single-polynomial requests.
 
     n = 2^U with U uniform in {8..16}, forward/inverse 50/50, int16 (q = 12289)
@@ -588,21 +587,24 @@ def run_serving(gb, seconds):
     buffers are pinned.  A saturating burst measures the capacity; open-loop
     Poisson arrivals at 50%, 90% and 100% of it give p50/p99 latency (submit to
     result in host memory).  A sample of requests is checked against the same
-    transform launched alone."""
+    transform launched alone.  The plans compute the headline's arithmetic."""
     import torch
 
     rng = np.random.default_rng(SEED + 1)
+    fl = gb.FLAG_CANONICAL if arith == "canonical" else 0
     plans, keys = [], {}
     for inv in (0, 1):
         for L in range(8, 13):
             n = 1 << L
             keys[(16, 12289, L, inv)] = len(plans)
-            plans.append(gb.Plan(gb.Kind.R2_I16_INV if inv else gb.Kind.R2_I16_FWD, n, 12289, pow(41, 4096 // n, 12289)))
+            plans.append(gb.Plan(gb.Kind.R2_I16_INV if inv else gb.Kind.R2_I16_FWD, n, 12289, pow(41, 4096 // n, 12289),
+                                 0, fl))
         for q, g in SERVE_Q32:
             for L in range(8, 17):
                 n = 1 << L
                 keys[(32, q, L, inv)] = len(plans)
-                plans.append(gb.Plan(gb.Kind.R2_I32_INV if inv else gb.Kind.R2_I32_FWD, n, q, pow(g, (q - 1) // n, q)))
+                plans.append(gb.Plan(gb.Kind.R2_I32_INV if inv else gb.Kind.R2_I32_FWD, n, q, pow(g, (q - 1) // n, q),
+                                     0, fl))
     pool = {}      # (dtype bits, q, L) -> pinned input polynomials
     for (bits, q, L, inv) in keys:
         if (bits, q, L) not in pool:
@@ -655,7 +657,7 @@ def run_serving(gb, seconds):
     cap = nsat / el
     out = {"workload": "single-polynomial requests: n=2^U, U~{8..16} (int16: {8..12}), fwd/inv 50/50, "
                        "int16 q=12289 / int32 q in {998244353,469762049,167772161,754974721} 50/50",
-           "plans": len(plans), "slots": 8, "api": "gbntt_server_* (pinned host buffers)",
+           "plans": len(plans), "slots": 8, "api": "gbntt_server_* (pinned host buffers)", "arithmetic": arith,
            "alone_vs_mix_checked": 256,
            "saturation": {"requests_per_s": cap, "NTT_per_s": cap, "algorithmic_GBps": nbytes / el / 1e9,
                           "requests": nsat, "microbatches": st["microbatches"], "launches": st["launches"],

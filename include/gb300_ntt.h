@@ -234,6 +234,8 @@ int gbntt_set_wait_limit(uint32_t polls);
 #define GBNTT_BQ_EL16     4   /* log2 coefficients per thread chosen for the int16 launch */
 #define GBNTT_BQ_FAMSET   5   /* design families compiled into the chosen int16 kernel (bit mask) */
 #define GBNTT_BQ_CTA      6   /* threads per CTA of the chosen int16 kernel */
+#define GBNTT_BQ_OCC      7   /* resident CTAs per SM the chosen int16 kernel's registers are budgeted
+                                 for (0: the width's default) */
 /* Setting the environment variable GBNTT_TUNE_LOG=1 prints the autotuner's
  * timing of every candidate configuration to stderr at batch creation;
  * GBNTT_TUNE_FORCE="<log2 coefficients per thread>,<CTAs per SM, 0 = default>"

@@ -638,6 +638,7 @@ int gbntt_batch_query(const gbntt_batch* b, int what, int64_t* value) {
         case GBNTT_BQ_EL16: if (!b->parts[i].i32) v = lay.cfg.elmax; break;
         case GBNTT_BQ_FAMSET: if (!b->parts[i].i32) v = lay.cfg.set; break;
         case GBNTT_BQ_CTA: if (!b->parts[i].i32) v = lay.cfg.cta; break;
+        case GBNTT_BQ_OCC: if (!b->parts[i].i32) v = lay.cfg.occ; break;
         default: return batch_fail(GBNTT_ERR_ARG, "unknown query");
         }
     }

@@ -12,6 +12,7 @@ const void* batch_kernels_c16(int el, int set, int occ) {
 #define GB_K(EL, OCC) \
     if (el == EL && occ == OCC) return reinterpret_cast<const void*>(&k_batch<false, BATCH_CTA, EL, C16, OCC>);
     GB_K(5, 0)
+    GB_K(5, 4)
     GB_K(4, 0)
     GB_K(4, 6)
     GB_K(4, 5)

@@ -33,8 +33,8 @@ constexpr Key kKeys[] = {
     {6, R4, 0}, {5, R4, 0}, {6, R2, 0}, {5, R2, 0}, {6, R8, 0}, {5, R8, 0}, {5, ALL16, 0},
     {4, R4, 0}, {4, R4, 5}, {4, R4, 6}, {4, R2, 0}, {4, R2, 5}, {4, R8, 0}, {4, R8, 5}, {4, ALL16, 0},
     // canonical families: 16 coefficients per thread at 4, 5 and 6 CTAs/SM, 32 at 3
-    // (8 per thread at 8 CTAs/SM spilled at its 32-register budget)
-    {4, C16, 6}, {4, C16, 5}, {4, C16, 0}, {5, C16, 0},
+    // and 4 (8 per thread at 8 CTAs/SM spilled at its 32-register budget)
+    {4, C16, 6}, {4, C16, 5}, {4, C16, 0}, {5, C16, 0}, {5, C16, 4},
 };
 constexpr int kN = (int)(sizeof(kKeys) / sizeof(kKeys[0]));
 BatchConfig kI16[kN];

@@ -734,18 +734,57 @@ int orc_execute(const orc_plan* p, const void* in, void* out, int64_t batch) {
     return 0;
 }
 
+/* the outputs of `count` polynomials reduced to [0, q) in place */
+static void reduce_canonical(const orc_plan* p, void* out, int64_t count) {
+    const int64_t total = count * (int64_t)p->n, q = p->q;
+    if (orc_elem_bytes(p) == 2) {
+        int16_t* y = (int16_t*)out;
+        for (int64_t i = 0; i < total; i++) {
+            int64_t r = y[i] % q;
+            y[i] = (int16_t)(r < 0 ? r + q : r);
+        }
+    } else {
+        int32_t* y = (int32_t*)out;
+        for (int64_t i = 0; i < total; i++) {
+            int64_t r = (int64_t)y[i] % q;
+            y[i] = (int32_t)(r < 0 ? r + q : r);
+        }
+    }
+}
+
 typedef struct {
     const orc_plan* p;
     const char* in;
     char* out;
     int64_t b0, b1;
+    int canonical;
 } mt_arg;
 
 static void* mt_worker(void* v) {
     mt_arg* a = (mt_arg*)v;
     size_t bytes = (size_t)a->p->n * (size_t)orc_elem_bytes(a->p);
     orc_execute(a->p, a->in + (size_t)a->b0 * bytes, a->out + (size_t)a->b0 * bytes, a->b1 - a->b0);
+    if (a->canonical) reduce_canonical(a->p, a->out + (size_t)a->b0 * bytes, a->b1 - a->b0);
     return NULL;
+}
+
+int orc_execute_mt2(const orc_plan* p, const void* in, void* out, int64_t batch, int nthreads, int canonical) {
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > batch) nthreads = (int)(batch > 0 ? batch : 1);
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
+    mt_arg* args = (mt_arg*)malloc(sizeof(mt_arg) * (size_t)nthreads);
+    for (int t = 0; t < nthreads; t++) {
+        args[t].p = p;
+        args[t].in = (const char*)in;
+        args[t].out = (char*)out;
+        args[t].b0 = batch * t / nthreads;
+        args[t].b1 = batch * (t + 1) / nthreads;
+        args[t].canonical = canonical;
+        pthread_create(&th[t], NULL, mt_worker, &args[t]);
+    }
+    for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    free(th); free(args);
+    return 0;
 }
 
 int orc_execute_mt(const orc_plan* p, const void* in, void* out, int64_t batch, int nthreads) {
@@ -759,6 +798,7 @@ int orc_execute_mt(const orc_plan* p, const void* in, void* out, int64_t batch, 
         args[t].out = (char*)out;
         args[t].b0 = batch * t / nthreads;
         args[t].b1 = batch * (t + 1) / nthreads;
+        args[t].canonical = 0;
         pthread_create(&th[t], NULL, mt_worker, &args[t]);
     }
     for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);

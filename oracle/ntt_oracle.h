@@ -83,6 +83,8 @@ int orc_run_layer(const orc_plan* p, int layer, const void* in, void* out);
 /* Run the whole pipeline on `batch` polynomials (contiguous). */
 int orc_execute(const orc_plan* p, const void* in, void* out, int64_t batch);
 int orc_execute_mt(const orc_plan* p, const void* in, void* out, int64_t batch, int nthreads);
+/* the same; canonical != 0 also reduces every output to [0, q), in each thread */
+int orc_execute_mt2(const orc_plan* p, const void* in, void* out, int64_t batch, int nthreads, int canonical);
 
 /* O(n^2) modular DFT, canonical residues.  out[k] = sum_j in[j] w^(+-jk). */
 void orc_dft(int n, int64_t q, int64_t root, int inverse, const int64_t* in, int64_t* out);

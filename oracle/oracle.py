@@ -41,6 +41,8 @@ def lib():
         L.orc_execute.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]
         L.orc_execute_mt.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                      ctypes.c_int]
+        L.orc_execute_mt2.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                      ctypes.c_int, ctypes.c_int]
         L.orc_dft.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
                               ctypes.c_void_p, ctypes.c_void_p]
         L.orc_ntt_exact.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
@@ -92,12 +94,16 @@ class Plan:
         assert rc == 0
         return y
 
-    def __call__(self, x, threads=1):
+    def __call__(self, x, threads=1, canonical=False):
+        """The pipeline on every polynomial of x; canonical: outputs reduced
+        to [0, q) (inside the worker threads)."""
         x = np.ascontiguousarray(x, dtype=self.dtype)
         assert x.size % self.n == 0
         y = np.empty_like(x)
         batch = x.size // self.n
-        if threads > 1:
+        if canonical:
+            lib().orc_execute_mt2(self.h, x.ctypes.data, y.ctypes.data, batch, max(1, threads), 1)
+        elif threads > 1:
             lib().orc_execute_mt(self.h, x.ctypes.data, y.ctypes.data, batch, threads)
         else:
             lib().orc_execute(self.h, x.ctypes.data, y.ctypes.data, batch)

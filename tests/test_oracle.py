@@ -231,3 +231,12 @@ def test_exact_transform_is_the_dft(orc, q, g, n):
     i = orc.ntt_exact(f, q, root, inverse=True)
     assert np.array_equal(i, np.stack([orc.dft(r[br], q, root, inverse=True) for r in f]))
     assert np.array_equal(i, (x % q) * n % q)
+
+
+@pytest.mark.parametrize("kind,n,q,root,dt", [(2, 1024, 12289, 11580, np.int16), (5, 256, 998244353, 476477967, np.int32)])
+def test_canonical_execution_reduces_in_threads(orc, kind, n, q, root, dt):
+    """Plan(x, canonical=True): the reference's outputs reduced to [0, q) in
+    the worker threads (the CPU arm of the canonical benchmark)."""
+    x = np.random.default_rng(n).integers(-q, q, (37, n)).astype(dt)
+    p = orc.Plan(kind, n, q, root)
+    assert np.array_equal(p(x, threads=4, canonical=True).astype(np.int64), p(x).astype(np.int64) % q)
