@@ -692,6 +692,8 @@ PROFILE_CASES = {
     "c_r2f16_1024": (0, 1024, 12289, 11580, 65536, 1),
     "c_r2i16_1024": (1, 1024, 12289, 11580, 65536, 1),
     "c_r2f32_4096": (4, 4096, 998244353, 63912897, 16384, 1),
+    "c_r2f16_256": (0, 256, 12289, pow(41, 16, 12289), 262144, 1),
+    "c_r2i16_256": (1, 256, 12289, pow(41, 16, 12289), 262144, 1),
     "c_r2g32_4096": (5, 4096, 998244353, 63912897, 16384, 1),
     "c_r2f32_16k": (4, 1 << 14, 998244353, 666702199, 4096, 1),
     "c_r2g32_16k": (5, 1 << 14, 998244353, 666702199, 4096, 1),

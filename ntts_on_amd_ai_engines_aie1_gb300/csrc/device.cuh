@@ -241,8 +241,11 @@ template <bool SCALE, int E>
 __device__ __forceinline__ void epilogue_all(int (&v)[E], const KArgs& a);
 
 // Canonical families: every lane to [0, q), or n^-1 times it (a Shoup
-// multiplication, [0, 2q), then one subtraction) for a scaled inverse.
-template <int E>
+// multiplication, [0, 2q), then one subtraction) for a scaled inverse.  (int32
+// lanes end below 4q, so two subtract-and-minimum steps would reduce them
+// without a multiply; measured mixed against the Barrett step, -4 % to +12 %
+// per design, so every family keeps the Barrett step.)
+template <bool I32, int E>
 __device__ __forceinline__ void epilogue_canon(int (&v)[E], const KArgs& a, bool scale) {
     const unsigned q = (unsigned)a.q;
     if (scale) {
@@ -260,7 +263,7 @@ __device__ __forceinline__ void epilogue_canon(int (&v)[E], const KArgs& a, bool
 template <int FAM, bool BR, int E>
 __device__ __forceinline__ void epilogue(int (&v)[E], const KArgs& a) {
     if constexpr (fam_canon(FAM)) {
-        epilogue_canon(v, a, fam_scales(FAM, BR) && a.scale);
+        epilogue_canon<FAM == F_C32F || FAM == F_C32I>(v, a, fam_scales(FAM, BR) && a.scale);
     } else {
         epilogue_all<fam_scales(FAM, BR)>(v, a);
     }
