@@ -12,6 +12,7 @@ const void* batch_kernels_i16_w32g(int el, int set, int occ);
 const void* batch_kernels_i16_w16(int el, int set, int occ);
 const void* batch_kernels_i16_w16g(int el, int set, int occ);
 const void* batch_kernels_c16(int el, int set, int occ);
+const void* batch_kernels_c16_small(int el, int set, int occ);
 const void* batch_zc_kernel_c16(int set, int el);
 
 namespace {
@@ -23,6 +24,7 @@ constexpr int C16 = (1 << F_C16F) | (1 << F_C16I);   // canonical forward + inve
 
 struct Key {
     int el, set, occ;
+    int cta = BATCH_CTA;
 };
 // 256-thread CTAs with 64, 32 or 16 coefficients per thread; the narrower
 // ones carry less unrolled code per variant and fit more CTAs per SM (occ:
@@ -35,6 +37,9 @@ constexpr Key kKeys[] = {
     // canonical families: 16 coefficients per thread at 4, 5 and 6 CTAs/SM, 32 at 3
     // and 4 (8 per thread at 8 CTAs/SM spilled at its 32-register budget)
     {4, C16, 6}, {4, C16, 5}, {4, C16, 0}, {5, C16, 0}, {5, C16, 4},
+    // 128-thread CTAs (tiles of 2048 coefficients, n <= 2^11 at 16 per thread):
+    // half the work per tile, so a batch's last wave of tiles ends sooner
+    {4, C16, 12, 128}, {4, C16, 10, 128},
 };
 constexpr int kN = (int)(sizeof(kKeys) / sizeof(kKeys[0]));
 BatchConfig kI16[kN];
@@ -45,12 +50,17 @@ int batch_configs_i16(const BatchConfig** out) {
         for (int i = 0; i < kN; ++i) {
             const Key k = kKeys[i];
             const void* fn = nullptr;
-            for (auto get : {batch_kernels_i16_w64, batch_kernels_i16_w32, batch_kernels_i16_w32g,
-                             batch_kernels_i16_w16, batch_kernels_i16_w16g, batch_kernels_c16})
-                if (!fn) fn = get(k.el, k.set, k.occ);
-            const void* zfn = k.set == C16 ? (k.occ == 0 ? batch_zc_kernel_c16(k.set, k.el) : nullptr)
-                                           : batch_zc_kernel_i16(k.set, k.el);
-            kI16[i] = BatchConfig{false, k.el, k.set, fn, zfn, BATCH_CTA, k.occ};
+            if (k.cta != BATCH_CTA) {
+                fn = batch_kernels_c16_small(k.el, k.set, k.occ);
+            } else {
+                for (auto get : {batch_kernels_i16_w64, batch_kernels_i16_w32, batch_kernels_i16_w32g,
+                                 batch_kernels_i16_w16, batch_kernels_i16_w16g, batch_kernels_c16})
+                    if (!fn) fn = get(k.el, k.set, k.occ);
+            }
+            const void* zfn = k.cta != BATCH_CTA ? nullptr
+                              : k.set == C16 ? (k.occ == 0 ? batch_zc_kernel_c16(k.set, k.el) : nullptr)
+                                             : batch_zc_kernel_i16(k.set, k.el);
+            kI16[i] = BatchConfig{false, k.el, k.set, fn, zfn, k.cta, k.occ};
         }
         return true;
     }();

@@ -264,3 +264,28 @@ def test_bounded_wait_timeout_is_reported(gb):
     torch.cuda.synchronize()
     b.status()
     assert torch.equal(y, want) and torch.equal(y32, want32)
+
+
+@pytest.mark.parametrize("force", ["4,6", "4,5", "4,0", "5,0", "5,4", "4,12", "4,10"])
+def test_canonical_batch_every_configuration(gb, orc, monkeypatch, force):
+    """Every compiled canonical int16 configuration, pinned with
+    GBNTT_TUNE_FORCE (16 or 32 coefficients per thread, 256- or 128-thread
+    CTAs), on a radix-4 / radix-2 batch of n = 256 and 1024, forward and
+    inverse: outputs against the exact transform."""
+    monkeypatch.setenv("GBNTT_TUNE_FORCE", force)
+    rng = np.random.default_rng(SEED + 60)
+    segs, wants = [], []
+    for kind, n, q, count in ((2, 1024, 12289, 301), (2, 256, 7681, 513), (1, 1024, 12289, 77), (0, 512, 10753, 40)):
+        root = root_for(q, n)
+        x = rng.integers(-32768, 32768, (count, n)).astype(np.int16)
+        d = torch.from_numpy(x).cuda()
+        segs.append((gb.Plan(kind, n, q, root, 0, gb.FLAG_CANONICAL), d, torch.full_like(d, 3)))
+        wants.append(orc.ntt_exact(x, q, root, inverse=kind == 1))
+    b = gb.Batch(segs)
+    el, occ = (int(v) for v in force.split(","))
+    assert b.query(4) == el and b.query(7) == occ
+    b.graph_launch()
+    torch.cuda.synchronize()
+    b.status()
+    for (_, _, y), w in zip(segs, wants):
+        assert np.array_equal(y.cpu().numpy().astype(np.int64), w)
