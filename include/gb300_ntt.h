@@ -121,11 +121,13 @@ int gbntt_plan_destroy(gbntt_plan* plan);
  * `stream` (a cudaStream_t; NULL = legacy default stream).  One kernel launch
  * per call, except the int32 designs with n >= 2^16 (up to 2^22), which run
  * two passes (column and row sub-transforms) per chunk of polynomials (at most
- * 64 MiB; 48 MiB for the canonical four-step, whose column pass moves 2D tiles
- * with the Tensor Memory Accelerator and whose row pass applies the four-step
- * twist).  The environment variable GBNTT_FOURSTEP_MIN_L (14, 15 or 16, read
+ * 96 MiB, which stays in L2 between the passes; the canonical four-step's
+ * column pass moves 2D tiles with the Tensor Memory Accelerator and its row
+ * pass applies the four-step twist).  The environment variable GBNTT_FOURSTEP_MIN_L (14, 15 or 16, read
  * once per process) moves the canonical int32 plans of n >= 2^that length to
- * the four-step (default 16: n = 2^14 and 2^15 run one CTA per polynomial). */
+ * the four-step (default 16: n = 2^14 and 2^15 run one CTA per polynomial);
+ * GBNTT_FOURSTEP_CHUNK_MB (8 .. 120, read once) sets the chunk size of both
+ * two-pass schedules. */
 int gbntt_execute(const gbntt_plan* plan, const void* d_in, void* d_out, uint64_t batch,
                   void* stream);
 

@@ -110,11 +110,14 @@ int launch(const gbntt_plan* p, const void* d_in, void* d_out, uint64_t batch, c
         g_launches.fetch_add((unsigned long long)nl, std::memory_order_relaxed);
         return GBNTT_OK;
     } else if (p->large.cols) {
-        // two passes per chunk of polynomials; a chunk (<= 64 MiB) stays in L2
-        // between its passes.  Forward: columns then rows; inverse: rows first.
+        // two passes per chunk of polynomials; a chunk (large_chunk_bytes())
+        // stays in L2 between its passes.  Forward: columns then rows; inverse:
+        // rows first.  Every launch after the call's first is a programmatic
+        // dependent launch.
         const LargeInfo& li = p->large;
         const long long n = (long long)p->hp.n;
-        long long chunk = (64LL << 20) / (n * 4);
+        long long chunk = large_chunk_bytes() / (n * 4);
+        int nl = 0;
         if (chunk < 1) chunk = 1;
         const bool inverse = (p->hp.kind == K_R2_I32_INV);
         for (long long p0 = 0; p0 < (long long)batch; p0 += chunk) {
@@ -133,16 +136,20 @@ int launch(const gbntt_plan* p, const void* d_in, void* d_out, uint64_t batch, c
             void* rargs_first[] = {&first, &L1};
             void* cargs_last[] = {&last, &L2};
             void* rargs_last[] = {&last, &L1};
-            const dim3 cgrid((unsigned)(np * ((1LL << li.L2) / li.cols_per_cta)));
-            const dim3 rgrid((unsigned)(((np << li.L1) + li.rows_per_cta - 1) / li.rows_per_cta));
+            const unsigned cgrid = (unsigned)(np * ((1LL << li.L2) / li.cols_per_cta));
+            const unsigned rgrid = (unsigned)(((np << li.L1) + li.rows_per_cta - 1) / li.rows_per_cta);
+            auto cols = [&](void** args) {
+                return launch_kernel(li.cols, cgrid, li.cols_threads, li.cols_smem, args, s, nl++ > 0);
+            };
+            auto rows = [&](void** args) {
+                return launch_kernel(li.rows, rgrid, li.rows_threads, li.rows_smem, args, s, nl++ > 0);
+            };
             if (!inverse) {
-                e = cudaLaunchKernel(li.cols, cgrid, dim3(li.cols_threads), cargs_first, li.cols_smem, s);
-                if (e == cudaSuccess)
-                    e = cudaLaunchKernel(li.rows, rgrid, dim3(li.rows_threads), rargs_last, li.rows_smem, s);
+                e = cols(cargs_first);
+                if (e == cudaSuccess) e = rows(rargs_last);
             } else {
-                e = cudaLaunchKernel(li.rows, rgrid, dim3(li.rows_threads), rargs_first, li.rows_smem, s);
-                if (e == cudaSuccess)
-                    e = cudaLaunchKernel(li.cols, cgrid, dim3(li.cols_threads), cargs_last, li.cols_smem, s);
+                e = rows(rargs_first);
+                if (e == cudaSuccess) e = cols(cargs_last);
             }
             if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
             g_launches.fetch_add(2, std::memory_order_relaxed);

@@ -67,19 +67,41 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
     __shared__ long long sh_next[2];
     __shared__ int sh_pending[2];
     __shared__ int sh_failed;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31;
     const long long total = b.total_tiles;
 
-    // segment of tile t, searched from segment `from`: a CTA's tiles come from
-    // the counter in increasing order, so its search never goes back
-    auto seg_of = [&](long long t, int from) {
-        int s = from < 0 ? 0 : from;
-        while (s + 1 < b.nsegs && __ldg(&b.segs[s + 1].tile0) <= t) ++s;
-        return s;
+    // Segment of tile t: the last segment whose first tile is <= t (tile0 does
+    // not decrease; segment 0 starts at tile 0), searched in [lo, nsegs), lo a
+    // segment known to start at or before t.
+    // seg_find: a whole warp, 32 candidates per round, so a round costs one
+    // load latency however many segments the batch has (a CTA's first tile).
+    auto seg_find = [&](long long t, int lo) {
+        int hi = b.nsegs;
+        while (hi - lo > 1) {
+            const int step = (hi - lo + 31) >> 5;
+            const int j = lo + step * lane;
+            const unsigned m = __ballot_sync(0xffffffffu, j < hi && __ldg(&b.segs[j].tile0) <= t);
+            lo += step * (31 - __clz(m));                 // lane 0 (j = lo) always qualifies
+            hi = min(hi, lo + step);
+        }
+        return lo;
     };
-    // thread 0: start the bulk load of tile t into buffer i
-    auto issue = [&](long long t, int i, int from) {
-        const SegDev* sd = &b.segs[seg_of(t, from)];
+    // seg_of: one thread; a CTA's tiles increase, so the common case is t still
+    // in segment lo (one load); past it, a binary search
+    auto seg_of = [&](long long t, int lo) {
+        int hi = b.nsegs;
+        if (lo + 1 >= hi || __ldg(&b.segs[lo + 1].tile0) > t) return lo;
+        ++lo;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(&b.segs[mid].tile0) <= t) lo = mid;
+            else hi = mid;
+        }
+        return lo;
+    };
+    // one thread: start the bulk load of tile t (segment s) into buffer i
+    auto issue = [&](long long t, int i, int s) {
+        const SegDev* sd = &b.segs[s];
         const long long lt = t - sd->tile0;
         const long long P = sd->polys_per_tile;
         const long long count = sd->a.batch;
@@ -90,35 +112,47 @@ __global__ void __launch_bounds__(CTA, OCC ? OCC : batch_min_blocks(I32, CTA, EL
         bulk_load(stage0 + i * stage_bytes, src, bytes, &bar[i]);
     };
 
+    // The first tile of a CTA is its block index (the grid never exceeds the
+    // tile count), the later ones come from the counter, offset by the grid:
+    // the first load leaves without waiting for an atomic, and the segment's
+    // arguments reach shared memory while it is in flight.
+    const long long t0 = (long long)blockIdx.x;
+    int cur_seg = -1;
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        const long long t0 = (long long)atomicAdd(&b.ctr[CTR_NEXT], 1ull);
-        sh_next[1] = t0;
         sh_pending[0] = 0;
         sh_pending[1] = 0;
         sh_failed = 0;
-        if (t0 < total) {
-            issue(t0, 0, 0);
+    }
+    if (t0 < total) {
+        const int s0 = seg_find(t0, 0);
+        if (tid == 0) {
+            issue(t0, 0, s0);
             sh_pending[0] = 1;
         }
+        const int* src = reinterpret_cast<const int*>(&b.segs[s0].a);
+        int* dst = reinterpret_cast<int*>(ka);
+        for (int w = tid; w < (int)(sizeof(KArgs) / 4); w += CTA) dst[w] = src[w];
+        cur_seg = s0;
     }
     __syncthreads();
-    long long t = sh_next[1];
+    long long t = t0;
     unsigned phases = 0u;    // bit i: parity of the next completion of bar[i]
     int buf = 0;
-    int cur_seg = -1;
     KC kc;
+    if (cur_seg >= 0) kc = make_kc(*ka);
     while (t < total) {
         const int s = seg_of(t, cur_seg);
         const SegDev* sd = &b.segs[s];
         if (tid == 0) {
-            const long long tn = (long long)atomicAdd(&b.ctr[CTR_NEXT], 1ull);
+            // claim the next tile and start its load into the other buffer
+            const long long tn = (long long)gridDim.x + (long long)atomicAdd(&b.ctr[CTR_NEXT], 1ull);
             sh_next[buf] = tn;
             if (tn < total) {
                 bulk_wait_read();           // the other buffer's last store has left shared memory
-                issue(tn, buf ^ 1, s);
+                issue(tn, buf ^ 1, seg_of(tn, s));
                 sh_pending[buf ^ 1] = 1;
             }
         }

@@ -1076,6 +1076,27 @@ cudaError_t launch_canon_large(const CanonLarge& li, const KArgs& base, const in
                                const int2* twist, const void* in, void* out, long long batch, bool inverse,
                                unsigned* err, cudaStream_t s, int* launches);
 
+// Programmatic dependent launch, for the launches of one call that depend on
+// one another (the two passes of a chunk, the chunks of a call): every launch
+// after the first carries the programmatic-stream-serialization attribute, so
+// its CTAs take the SM slots the previous grid's last CTAs free, with no
+// launch gap.  Each such kernel starts with grid_dep_start(): it lets its own
+// dependent launch proceed (safe this early, since the dependent's wait
+// covers this whole grid and its memory operations) and waits for the
+// previous grid's results before touching global memory.  Without the
+// attribute both instructions are no-ops.
+__device__ __forceinline__ void grid_dep_start() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+// kernels_misc.cu: fn on stream s, as a programmatic dependent launch when `dependent`
+cudaError_t launch_kernel(const void* fn, unsigned grid, int threads, int smem, void** args, cudaStream_t s,
+                          bool dependent);
+// the polynomials of a call go through the two passes of the long int32
+// transforms in chunks of at most this many bytes, so the intermediate stays
+// in L2 (96 MiB; GBNTT_FOURSTEP_CHUNK_MB, 8 .. 120, read once per process)
+long long large_chunk_bytes();
+
 // single-purpose kernels (kernels_misc.cu)
 cudaError_t launch_r8_stage(const KArgs& a, int L, cudaStream_t s);
 cudaError_t launch_bitrev(const KArgs& a, int L, cudaStream_t s);

@@ -11,7 +11,7 @@
 //      the row,
 // and the inverse (bit-reversed in, natural out, no n^-1) runs the inverse
 // steps in the opposite order: rows, untwist by root^-(c bitrev(r)), columns.
-// Polynomials go through both passes in chunks of at most CHUNK_BYTES, so the
+// Polynomials go through both passes in chunks of at most large_chunk_bytes(), so the
 // intermediate stays in L2 between the passes.
 //
 // The column pass moves 2D tiles (COLS adjacent columns x n1 rows) between
@@ -32,7 +32,6 @@ namespace gbntt {
 
 namespace {
 
-constexpr long long CHUNK_BYTES = 48LL << 20;
 constexpr int ROW_EL = 4;            // 16 coefficients per thread in the row pass
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int c, int r,
@@ -74,6 +73,7 @@ __global__ void __launch_bounds__(COLS << (L1 - EL))
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
+    grid_dep_start();
     if (tid == 0) {
         mbar_expect_tx(bar, N1 * COLS * 4);
 #pragma unroll
@@ -120,6 +120,7 @@ __global__ void __launch_bounds__(P << (L2 - EL)) k_crows(const __grid_constant_
     static_assert((FWD ? LO0 : LOZ) == L2 - EL, "twist layout");
     static_assert((FWD ? LOZ : LO0) == 0, "contiguous runs on the other side");
     extern __shared__ int rsm[];
+    grid_dep_start();
     const int tid = threadIdx.x, lp = tid / G, g = tid % G;
     const long long row = row0 + (long long)blockIdx.x * P + lp;
     const bool active = row < row0 + rows;
@@ -282,7 +283,7 @@ cudaError_t launch_canon_large(const CanonLarge& li, const KArgs& base, const in
     } else {
         map_in = map_out;
     }
-    long long chunk = CHUNK_BYTES / (n * 4);
+    long long chunk = large_chunk_bytes() / (n * 4);
     if (chunk < 1) chunk = 1;
     const long long tpp = n2 / li.cols_width;
     KArgs ac = base, ar = base;
@@ -294,16 +295,21 @@ cudaError_t launch_canon_large(const CanonLarge& li, const KArgs& base, const in
         const long long np = chunk < batch - p0 ? chunk : batch - p0;
         const long long tile0 = p0 * tpp, row0 = p0 * n1, rows = np * n1;
         int L1 = li.L1;
+        // the first launch of the call follows the stream's previous work as
+        // usual; every later one is a programmatic dependent launch
+        auto launch = [&](const void* fn, unsigned grid, int threads, int smem, void** args) {
+            return launch_kernel(fn, grid, threads, smem, args, s, nl++ > 0);
+        };
         auto cols = [&]() {
             void* args[] = {&map_in, &map_out, &ac, const_cast<int*>(&n2), const_cast<long long*>(&tile0), &err};
-            return cudaLaunchKernel(li.cols, dim3((unsigned)(np * tpp)), dim3(li.cols_threads), args, li.cols_smem, s);
+            return launch(li.cols, (unsigned)(np * tpp), li.cols_threads, li.cols_smem, args);
         };
         auto rowsk = [&](const void* src) {
             ar.in = src;
             ar.out = out;
             void* args[] = {&ar, &L1, const_cast<long long*>(&row0), const_cast<long long*>(&rows)};
-            return cudaLaunchKernel(li.rows, dim3((unsigned)((rows + li.rows_per_cta - 1) / li.rows_per_cta)),
-                                    dim3(li.rows_threads), args, li.rows_smem, s);
+            return launch(li.rows, (unsigned)((rows + li.rows_per_cta - 1) / li.rows_per_cta), li.rows_threads,
+                          li.rows_smem, args);
         };
         if (!inverse) {
             e = cols();
@@ -313,7 +319,6 @@ cudaError_t launch_canon_large(const CanonLarge& li, const KArgs& base, const in
             if (e == cudaSuccess) e = cols();
         }
         if (e != cudaSuccess) return e;
-        nl += 2;
     }
     if (launches) *launches = nl;
     return cudaSuccess;

@@ -26,6 +26,7 @@ __global__ void __launch_bounds__(COLS << (L1 - LARGE_EL)) k_cols(const __grid_c
     constexpr int EL = LARGE_EL, G = 1 << (L1 - EL), E = 1 << EL, NS = nsteps(FAM, L1);
     constexpr int LO0 = window_lo(FAM, L1, EL, 0), LOZ = window_lo(FAM, L1, EL, NS - 1);
     extern __shared__ int csmem[];
+    grid_dep_start();
     const int tid = threadIdx.x, cl = tid % COLS, g = tid / COLS;
     const long long blocks_per_poly = (1LL << L2) / COLS;
     const long long poly = blockIdx.x / blocks_per_poly;
@@ -50,6 +51,7 @@ __global__ void __launch_bounds__(P << (L2 - LARGE_EL)) k_rows(const __grid_cons
     constexpr int EL = LARGE_EL, G = 1 << (L2 - EL), E = 1 << EL, NS = nsteps(FAM, L2), N = 1 << L2;
     constexpr int LO0 = window_lo(FAM, L2, EL, 0), LOZ = window_lo(FAM, L2, EL, NS - 1);
     extern __shared__ int rsmem[];
+    grid_dep_start();
     const int tid = threadIdx.x, lp = tid / G, g = tid % G;
     const long long row = (long long)blockIdx.x * P + lp;        // rows of all polynomials, in order
     const bool active = row < (a.batch << L1);

@@ -1,5 +1,7 @@
 // kernels_misc.cu -- the single-pass designs: one radix-8 stage, the
 // bit-reversal unit and the full Barrett multiplication by a constant.
+#include <cstdlib>
+
 #include "device.cuh"
 
 namespace gbntt {
@@ -155,5 +157,29 @@ cudaError_t launch_full_barrett(const KArgs& a, long long total, int fs, int wq,
 }
 
 const void* bitrev_kernel_ptr() { return reinterpret_cast<const void*>(&k_bitrev); }
+
+cudaError_t launch_kernel(const void* fn, unsigned grid, int threads, int smem, void** args, cudaStream_t s,
+                          bool dependent) {
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = (size_t)smem;
+    cfg.stream = s;
+    cfg.attrs = dependent ? attr : nullptr;
+    cfg.numAttrs = dependent ? 1 : 0;
+    return cudaLaunchKernelExC(&cfg, fn, args);
+}
+
+long long large_chunk_bytes() {
+    static const long long v = [] {
+        const char* e = std::getenv("GBNTT_FOURSTEP_CHUNK_MB");
+        const long long x = e ? std::atoll(e) : 96;
+        return (x >= 8 && x <= 120 ? x : 96) << 20;
+    }();
+    return v;
+}
 
 }  // namespace gbntt

@@ -289,3 +289,37 @@ def test_canonical_batch_every_configuration(gb, orc, monkeypatch, force):
     b.status()
     for (_, _, y), w in zip(segs, wants):
         assert np.array_equal(y.cpu().numpy().astype(np.int64), w)
+
+
+def test_many_segments_one_launch_per_part(gb):
+    """300 small segments (radix-2/4, forward/inverse, lane and canonical
+    arithmetic, n = 16 .. 1024, 1-9 polynomials each, some empty) in one
+    persistent launch per part: every CTA finds its first tile's segment and
+    later segments by search, not by walking the list; outputs against the
+    per-plan launches."""
+    rng = np.random.default_rng(SEED + 70)
+    plans = {}
+    segs, wants = [], []
+    for i in range(300):
+        kind = int(rng.choice([0, 1, 2]))
+        L = int(rng.integers(4, 11))
+        if kind == 2 and L % 2:
+            L -= 1
+        n, q = 1 << L, int(rng.choice([12289, 12289, 7681])) if L <= 8 else 12289
+        flags = int(rng.integers(0, 2))              # lane or canonical arithmetic
+        key = (kind, n, q, flags)
+        if key not in plans:
+            plans[key] = gb.Plan(kind, n, q, root_for(q, n), 0, flags)
+        count = 0 if i % 37 == 5 else int(rng.integers(1, 10))
+        x = torch.from_numpy(rng.integers(-32768, 32768, (count, n)).astype(np.int16)).cuda()
+        segs.append((plans[key], x, torch.full_like(x, 11)))
+        wants.append(plans[key](x) if count else x.clone())
+    b = gb.Batch(segs)
+    assert b.launches == 2                           # int16 lanes, int16 canonical
+    for rep in range(2):
+        b.graph_launch()
+        torch.cuda.synchronize()
+        b.status()
+        for i, ((_, x, y), w) in enumerate(zip(segs, wants)):
+            if x.shape[0]:
+                assert torch.equal(y, w), (i, rep)

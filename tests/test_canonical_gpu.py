@@ -222,15 +222,17 @@ def test_canonical_int32_four_step(gb, orc, q, L):
 
 
 def test_canonical_four_step_status_and_many_chunks(gb, orc):
-    """A batch spanning several L2 chunks (48 MiB each) and the plan's status call."""
+    """A batch spanning three L2 chunks (96 MiB, 24 polynomials of 2^20, each;
+    programmatic dependent launches between the passes and the chunks) and the
+    plan's status call."""
     q, n = 469762049, 1 << 20
     root = root_for(q, n)
-    x = np.random.default_rng(SEED + 3990).integers(0, q, (26, n)).astype(np.int32)
+    x = np.random.default_rng(SEED + 3990).integers(0, q, (50, n)).astype(np.int32)
     plan = gb.Plan(4, n, q, root, 0, gb.FLAG_CANONICAL)
     t = torch.from_numpy(x).cuda()
     y = plan(t)
     torch.cuda.synchronize()
     plan.status()
     got = y.cpu().numpy()
-    for i in (0, 11, 12, 25):
+    for i in (0, 23, 24, 47, 48, 49):
         assert np.array_equal(got[i].astype(np.int64), orc.ntt_exact(x[i:i + 1], q, root)[0])

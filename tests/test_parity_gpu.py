@@ -431,6 +431,20 @@ def test_r2_i32_two_pass(gb, orc, q, L):
     assert np.array_equal(got, z)
 
 
+def test_r2_i32_two_pass_many_chunks(gb):
+    """50 polynomials of 2^20 (three 96 MiB chunks, programmatic dependent
+    launches between the passes and the chunks), forward and inverse: the
+    polynomials at the chunk boundaries equal their single-polynomial calls."""
+    q, n = 998244353, 1 << 20
+    root = root_for(q, n)
+    x = torch.from_numpy(np.random.default_rng(SEED + 1300).integers(0, q, (50, n)).astype(np.int32)).cuda()
+    for kind in (gb.Kind.R2_I32_FWD, gb.Kind.R2_I32_INV):
+        plan = gb.Plan(kind, n, q, root)
+        y = plan(x)
+        for i in (0, 23, 24, 47, 48, 49):
+            assert torch.equal(y[i:i + 1], plan(x[i:i + 1])), (kind, i)
+
+
 def test_r2_i32_two_pass_dft_column(gb, orc):
     """n = 2^16 against the modular DFT at a few output positions."""
     q, n = 469762049, 1 << 16
