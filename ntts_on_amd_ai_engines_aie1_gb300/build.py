@@ -15,7 +15,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libgb300ntt.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["abi.cu", "batch.cu", "batch_k16.cu", "batch_k16_w64.cu", "batch_k16_w32.cu", "batch_k16_w32g.cu", "batch_k16_w16.cu", "batch_k16_w16g.cu", "batch_k16_zc.cu", "batch_k32.cu", "batch_k32_w16.cu", "noalloc.cu", "kernels_r2.cu", "kernels_r2_32.cu", "kernels_r4_r8.cu", "kernels_misc.cu", "kernels_large.cu", "serve.cu", "canon_tables.cu", "kernels_c16.cu", "kernels_c32.cu", "batch_c16.cu", "batch_c32.cu", "kernels_c32_large.cu"]
+CUDA_SOURCES = ["abi.cu", "batch.cu", "batch_k16.cu", "batch_k16_w64.cu", "batch_k16_w32.cu", "batch_k16_w32g.cu", "batch_k16_w16.cu", "batch_k16_w16g.cu", "batch_k16_zc.cu", "batch_k32.cu", "batch_k32_w16.cu", "noalloc.cu", "kernels_r2.cu", "kernels_r2_32.cu", "kernels_r4_r8.cu", "kernels_misc.cu", "kernels_large.cu", "serve.cu", "canon_tables.cu", "kernels_c16.cu", "kernels_c32.cu", "batch_c16.cu", "batch_c16_small.cu", "batch_c32.cu", "kernels_c32_large.cu"]
 CXX_SOURCES = ["tables.cpp"]
 
 

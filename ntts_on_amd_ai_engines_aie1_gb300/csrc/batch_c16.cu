@@ -20,14 +20,6 @@ const void* batch_kernels_c16(int el, int set, int occ) {
     return nullptr;
 }
 
-// 128-thread CTAs
-const void* batch_kernels_c16_small(int el, int set, int occ) {
-    constexpr int C16 = (1 << F_C16F) | (1 << F_C16I);
-    if (set == C16 && el == 4 && occ == 12) return reinterpret_cast<const void*>(&k_batch<false, 128, 4, C16, 12>);
-    if (set == C16 && el == 4 && occ == 10) return reinterpret_cast<const void*>(&k_batch<false, 128, 4, C16, 10>);
-    return nullptr;
-}
-
 const void* batch_zc_kernel_c16(int set, int el) {
     constexpr int C16 = (1 << F_C16F) | (1 << F_C16I);
     if (set == C16 && el == 4) return reinterpret_cast<const void*>(&k_batch_zc<false, BATCH_CTA, 4, C16>);

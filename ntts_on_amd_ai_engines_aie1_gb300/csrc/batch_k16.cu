@@ -1,7 +1,8 @@
 // batch_k16.cu -- the configuration table of the int16 persistent kernels.
 // The kernels are instantiated in batch_k16_w64.cu, batch_k16_w32.cu,
-// batch_k16_w32g.cu, batch_k16_w16.cu and batch_k16_w16g.cu (compiled in
-// parallel); the zero-copy forms in batch_k16_zc.cu.
+// batch_k16_w32g.cu, batch_k16_w16.cu, batch_k16_w16g.cu, batch_c16.cu and
+// batch_c16_small.cu (compiled in parallel); the zero-copy forms in
+// batch_k16_zc.cu.
 #include "batch_kernel.cuh"
 
 namespace gbntt {
@@ -12,7 +13,7 @@ const void* batch_kernels_i16_w32g(int el, int set, int occ);
 const void* batch_kernels_i16_w16(int el, int set, int occ);
 const void* batch_kernels_i16_w16g(int el, int set, int occ);
 const void* batch_kernels_c16(int el, int set, int occ);
-const void* batch_kernels_c16_small(int el, int set, int occ);
+const void* batch_kernels_c16_small(int el, int set, int occ, int cta);
 const void* batch_zc_kernel_c16(int set, int el);
 
 namespace {
@@ -40,6 +41,9 @@ constexpr Key kKeys[] = {
     // 128-thread CTAs (tiles of 2048 coefficients, n <= 2^11 at 16 per thread):
     // half the work per tile, so a batch's last wave of tiles ends sooner
     {4, C16, 12, 128}, {4, C16, 10, 128},
+    // 32 coefficients per thread in 64-thread CTAs (n <= 2^11): one warp per
+    // 1024-point polynomial (the fastest on batches of 4x the benchmark's)
+    {5, C16, 12, 64},
 };
 constexpr int kN = (int)(sizeof(kKeys) / sizeof(kKeys[0]));
 BatchConfig kI16[kN];
@@ -51,7 +55,7 @@ int batch_configs_i16(const BatchConfig** out) {
             const Key k = kKeys[i];
             const void* fn = nullptr;
             if (k.cta != BATCH_CTA) {
-                fn = batch_kernels_c16_small(k.el, k.set, k.occ);
+                fn = batch_kernels_c16_small(k.el, k.set, k.occ, k.cta);
             } else {
                 for (auto get : {batch_kernels_i16_w64, batch_kernels_i16_w32, batch_kernels_i16_w32g,
                                  batch_kernels_i16_w16, batch_kernels_i16_w16g, batch_kernels_c16})

@@ -266,11 +266,11 @@ def test_bounded_wait_timeout_is_reported(gb):
     assert torch.equal(y, want) and torch.equal(y32, want32)
 
 
-@pytest.mark.parametrize("force", ["4,6", "4,5", "4,0", "5,0", "5,4", "4,12", "4,10"])
+@pytest.mark.parametrize("force", ["4,6", "4,5", "4,0", "5,0", "5,4", "4,12", "4,10", "5,12"])
 def test_canonical_batch_every_configuration(gb, orc, monkeypatch, force):
     """Every compiled canonical int16 configuration, pinned with
-    GBNTT_TUNE_FORCE (16 or 32 coefficients per thread, 256- or 128-thread
-    CTAs), on a radix-4 / radix-2 batch of n = 256 and 1024, forward and
+    GBNTT_TUNE_FORCE (16 or 32 coefficients per thread, CTAs of 256, 128 or
+    64 threads), on a radix-4 / radix-2 batch of n = 256 and 1024, forward and
     inverse: outputs against the exact transform."""
     monkeypatch.setenv("GBNTT_TUNE_FORCE", force)
     rng = np.random.default_rng(SEED + 60)
