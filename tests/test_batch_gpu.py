@@ -323,3 +323,31 @@ def test_many_segments_one_launch_per_part(gb):
         for i, ((_, x, y), w) in enumerate(zip(segs, wants)):
             if x.shape[0]:
                 assert torch.equal(y, w), (i, rep)
+
+
+def test_batch_graph_with_two_pass_segments(gb):
+    """Segments that run their plan's own launches inside a batch's CUDA graph:
+    the canonical int32 four-step (n = 2^16) and the lane two-pass (n = 2^17),
+    whose launches after the first are programmatic dependent launches, beside
+    a persistent int16 segment; replayed twice, against the plans' own calls."""
+    rng = np.random.default_rng(SEED + 80)
+    specs = [(4, 1 << 16, 998244353, 5, gb.FLAG_CANONICAL), (5, 1 << 17, 469762049, 3, 0),
+             (2, 1024, 12289, 700, gb.FLAG_CANONICAL)]
+    segs, wants = [], []
+    for kind, n, q, count, fl in specs:
+        dt = np.int16 if q == 12289 else np.int32
+        plan = gb.Plan(kind, n, q, root_for(q, n), 0, fl)
+        x = torch.from_numpy(rng.integers(0, q, (count, n)).astype(dt)).cuda()
+        segs.append((plan, x, torch.full_like(x, 9)))
+        wants.append(plan(x))
+    b = gb.Batch(segs)
+    s = torch.cuda.Stream()
+    for rep in range(2):
+        for _, _, y in segs:
+            y.fill_(9)
+        torch.cuda.synchronize()
+        b.graph_launch(s)
+        s.synchronize()
+        b.status()
+        for i, ((_, _, y), w) in enumerate(zip(segs, wants)):
+            assert torch.equal(y, w), (i, rep)
