@@ -236,3 +236,40 @@ def test_canonical_four_step_status_and_many_chunks(gb, orc):
     got = y.cpu().numpy()
     for i in (0, 23, 24, 47, 48, 49):
         assert np.array_equal(got[i].astype(np.int64), orc.ntt_exact(x[i:i + 1], q, root)[0])
+
+
+def test_four_step_chunk_size_setting(gb, tmp_path):
+    """GBNTT_FOURSTEP_CHUNK_MB (read once per process): a child process with
+    8 MiB chunks (two polynomials of 2^20 per chunk, so eleven chunks and 21
+    dependent launches for 11 polynomials) gives the outputs of this process's
+    default chunks, for the canonical four-step and the lane two-pass."""
+    import os
+    import subprocess
+    import sys
+    q, n, count = 998244353, 1 << 20, 11
+    root = root_for(q, n)
+    x = np.random.default_rng(SEED + 4100).integers(0, q, (count, n)).astype(np.int32)
+    np.save(tmp_path / "x.npy", x)
+    want = {}
+    for name, kind, fl in (("canon_fwd", 4, gb.FLAG_CANONICAL), ("canon_inv", 5, gb.FLAG_CANONICAL),
+                           ("lane_fwd", 4, 0), ("lane_inv", 5, 0)):
+        want[name] = gb.Plan(kind, n, q, root, 0, fl)(torch.from_numpy(x).cuda()).cpu().numpy()
+    root_dir = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    child = f"""
+import numpy as np, torch, sys
+sys.path.insert(0, {root_dir!r})
+import ntts_on_amd_ai_engines_aie1_gb300 as gb
+x = torch.from_numpy(np.load({str(tmp_path / "x.npy")!r})).cuda()
+for name, kind, fl in (("canon_fwd", 4, gb.FLAG_CANONICAL), ("canon_inv", 5, gb.FLAG_CANONICAL),
+                       ("lane_fwd", 4, 0), ("lane_inv", 5, 0)):
+    p = gb.Plan(kind, {n}, {q}, {root}, 0, fl)
+    y = p(x)
+    torch.cuda.synchronize()
+    p.status()
+    np.save({str(tmp_path)!r} + "/" + name + ".npy", y.cpu().numpy())
+"""
+    env = dict(os.environ, GBNTT_FOURSTEP_CHUNK_MB="8")
+    r = subprocess.run([sys.executable, "-c", child], env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    for name, w in want.items():
+        assert np.array_equal(np.load(tmp_path / (name + ".npy")), w), name
