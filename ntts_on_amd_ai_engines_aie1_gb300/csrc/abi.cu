@@ -112,12 +112,10 @@ int launch(const gbntt_plan* p, const void* d_in, void* d_out, uint64_t batch, c
     } else if (p->large.cols) {
         // two passes per chunk of polynomials; a chunk (large_chunk_bytes())
         // stays in L2 between its passes.  Forward: columns then rows; inverse:
-        // rows first.  Every launch after the call's first is a programmatic
-        // dependent launch.
+        // rows first.  Programmatic dependent launches (grid_dep_start).
         const LargeInfo& li = p->large;
         const long long n = (long long)p->hp.n;
         long long chunk = large_chunk_bytes() / (n * 4);
-        int nl = 0;
         if (chunk < 1) chunk = 1;
         const bool inverse = (p->hp.kind == K_R2_I32_INV);
         for (long long p0 = 0; p0 < (long long)batch; p0 += chunk) {
@@ -139,10 +137,10 @@ int launch(const gbntt_plan* p, const void* d_in, void* d_out, uint64_t batch, c
             const unsigned cgrid = (unsigned)(np * ((1LL << li.L2) / li.cols_per_cta));
             const unsigned rgrid = (unsigned)(((np << li.L1) + li.rows_per_cta - 1) / li.rows_per_cta);
             auto cols = [&](void** args) {
-                return launch_kernel(li.cols, cgrid, li.cols_threads, li.cols_smem, args, s, nl++ > 0);
+                return launch_kernel(li.cols, cgrid, li.cols_threads, li.cols_smem, args, s, true);
             };
             auto rows = [&](void** args) {
-                return launch_kernel(li.rows, rgrid, li.rows_threads, li.rows_smem, args, s, nl++ > 0);
+                return launch_kernel(li.rows, rgrid, li.rows_threads, li.rows_smem, args, s, true);
             };
             if (!inverse) {
                 e = cols(cargs_first);
@@ -173,7 +171,7 @@ int launch(const gbntt_plan* p, const void* d_in, void* d_out, uint64_t batch, c
         if (blocks > 0x7FFFFFFFull) return fail(GBNTT_ERR_ARG, "batch too large for one launch");
         a.tab_bytes = blocks <= (unsigned long long)sms ? (int)p->tab_bytes : 0;
         void* args[] = {&a};
-        e = cudaLaunchKernel(k.fn, dim3((unsigned)blocks), dim3(k.threads), args, k.smem, s);
+        e = launch_kernel(k.fn, (unsigned)blocks, k.threads, k.smem, args, s, true);
     } else if (p->hp.kind == K_R8_I16_STAGE) {
         e = launch_r8_stage(a, p->hp.L, s);
     } else if (p->hp.kind == K_BITREV_I16) {

@@ -42,6 +42,21 @@ __host__ __device__ constexpr bool fam_canon(int fam) { return fam >= F_C16F && 
 
 // Per-launch arguments (by value; the kernel reads the constants from the
 // parameter bank).
+// Programmatic dependent launch.  The library's per-plan launches (every
+// design's kernel, the two passes of a long transform and its chunks; not the
+// persistent batch kernels) carry the programmatic-stream-serialization attribute, so
+// when the previous operation is a grid that has signalled
+// launch_dependents, their CTAs take the SM slots its last CTAs free, with no
+// launch gap.  Every such kernel starts with grid_dep_start(): it signals its
+// own dependents (safe this early: their wait covers this whole grid and its
+// memory operations) and waits for the previous grid's completion and results
+// before touching global memory.  After any other operation, or without the
+// attribute, the launch is ordered as usual and both instructions are no-ops.
+__device__ __forceinline__ void grid_dep_start() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 struct KArgs {
     const void* in;
     void* out;
@@ -970,11 +985,13 @@ __host__ __device__ constexpr bool kntt_two_ctas(int fam, int threads) {
 
 template <int FAM, int L, int EL, int P, bool BR>
 __global__ void __launch_bounds__(P << (L - EL)) k_ntt(const __grid_constant__ KArgs a) {
+    grid_dep_start();
     k_ntt_body<FAM, L, EL, P, BR>(a);
 }
 
 template <int FAM, int L, int EL, int P, bool BR>
 __global__ void __launch_bounds__(P << (L - EL), 2) k_ntt2(const __grid_constant__ KArgs a) {
+    grid_dep_start();
     k_ntt_body<FAM, L, EL, P, BR>(a);
 }
 
@@ -1076,20 +1093,8 @@ cudaError_t launch_canon_large(const CanonLarge& li, const KArgs& base, const in
                                const int2* twist, const void* in, void* out, long long batch, bool inverse,
                                unsigned* err, cudaStream_t s, int* launches);
 
-// Programmatic dependent launch, for the launches of one call that depend on
-// one another (the two passes of a chunk, the chunks of a call): every launch
-// after the first carries the programmatic-stream-serialization attribute, so
-// its CTAs take the SM slots the previous grid's last CTAs free, with no
-// launch gap.  Each such kernel starts with grid_dep_start(): it lets its own
-// dependent launch proceed (safe this early, since the dependent's wait
-// covers this whole grid and its memory operations) and waits for the
-// previous grid's results before touching global memory.  Without the
-// attribute both instructions are no-ops.
-__device__ __forceinline__ void grid_dep_start() {
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-}
-// kernels_misc.cu: fn on stream s, as a programmatic dependent launch when `dependent`
+// kernels_misc.cu: fn on stream s, as a programmatic dependent launch when
+// `dependent` (see grid_dep_start)
 cudaError_t launch_kernel(const void* fn, unsigned grid, int threads, int smem, void** args, cudaStream_t s,
                           bool dependent);
 // the polynomials of a call go through the two passes of the long int32

@@ -295,10 +295,10 @@ cudaError_t launch_canon_large(const CanonLarge& li, const KArgs& base, const in
         const long long np = chunk < batch - p0 ? chunk : batch - p0;
         const long long tile0 = p0 * tpp, row0 = p0 * n1, rows = np * n1;
         int L1 = li.L1;
-        // the first launch of the call follows the stream's previous work as
-        // usual; every later one is a programmatic dependent launch
+        // programmatic dependent launches (grid_dep_start)
         auto launch = [&](const void* fn, unsigned grid, int threads, int smem, void** args) {
-            return launch_kernel(fn, grid, threads, smem, args, s, nl++ > 0);
+            ++nl;
+            return launch_kernel(fn, grid, threads, smem, args, s, true);
         };
         auto cols = [&]() {
             void* args[] = {&map_in, &map_out, &ac, const_cast<int*>(&n2), const_cast<long long*>(&tile0), &err};

@@ -14,6 +14,7 @@ namespace {
 // int32, reduces y_k with twiddle root^(i k) and writes the eight results
 // (de-interleaved and 3-bit reversed, :152-154) as one 16-byte store at 8 i.
 __global__ void __launch_bounds__(256) k_r8_stage(const KArgs a, int L) {
+    grid_dep_start();
     const int n = 1 << L, M = n >> 3;
     const long long total = a.batch << (L - 3);
     const short* in = static_cast<const short*>(a.in);
@@ -73,6 +74,7 @@ __global__ void __launch_bounds__(256) k_r8_stage(const KArgs a, int L) {
 // with coalesced 16-byte loads, then written back in order, each thread
 // reading the bit-reversed source position from shared memory.
 __global__ void __launch_bounds__(256) k_bitrev(const KArgs a, int L, int P) {
+    grid_dep_start();
     extern __shared__ short sb[];
     const int n = 1 << L;
     const long long poly0 = (long long)blockIdx.x * P;
@@ -95,6 +97,7 @@ __global__ void __launch_bounds__(256) k_bitrev(const KArgs a, int L, int P) {
 }
 
 __global__ void __launch_bounds__(256) k_full_barrett(const KArgs a, long long total, int fs, int wq) {
+    grid_dep_start();
     const short* in = static_cast<const short*>(a.in);
     short* out = static_cast<short*>(a.out);
     const long long nvec = total >> 3;
@@ -138,8 +141,9 @@ int bitrev_smem_bytes(int L) {
 
 cudaError_t launch_r8_stage(const KArgs& a, int L, cudaStream_t s) {
     const long long work = a.batch << (L - 3);
-    k_r8_stage<<<grid_for(work, 256), 256, 0, s>>>(a, L);
-    return cudaGetLastError();
+    KArgs ka = a;
+    void* args[] = {&ka, &L};
+    return launch_kernel(reinterpret_cast<const void*>(&k_r8_stage), grid_for(work, 256), 256, 0, args, s, true);
 }
 
 cudaError_t launch_bitrev(const KArgs& a, int L, cudaStream_t s) {
@@ -147,13 +151,17 @@ cudaError_t launch_bitrev(const KArgs& a, int L, cudaStream_t s) {
     const int P = n >= 8192 ? 1 : 8192 / n;
     const long long blocks = (a.batch + P - 1) / P;
     const int smem = P * n * 2;
-    k_bitrev<<<(unsigned)blocks, 256, smem, s>>>(a, L, P);
-    return cudaGetLastError();
+    KArgs ka = a;
+    int Lv = L, Pv = P;
+    void* args[] = {&ka, &Lv, &Pv};
+    return launch_kernel(reinterpret_cast<const void*>(&k_bitrev), (unsigned)blocks, 256, smem, args, s, true);
 }
 
 cudaError_t launch_full_barrett(const KArgs& a, long long total, int fs, int wq, cudaStream_t s) {
-    k_full_barrett<<<grid_for((total + 7) / 8, 256), 256, 0, s>>>(a, total, fs, wq);
-    return cudaGetLastError();
+    KArgs ka = a;
+    void* args[] = {&ka, &total, &fs, &wq};
+    return launch_kernel(reinterpret_cast<const void*>(&k_full_barrett), grid_for((total + 7) / 8, 256), 256, 0, args,
+                         s, true);
 }
 
 const void* bitrev_kernel_ptr() { return reinterpret_cast<const void*>(&k_bitrev); }
