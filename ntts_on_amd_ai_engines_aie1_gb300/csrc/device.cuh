@@ -40,12 +40,10 @@ enum Fam {
 };
 __host__ __device__ constexpr bool fam_canon(int fam) { return fam >= F_C16F && fam <= F_C32I; }
 
-// Per-launch arguments (by value; the kernel reads the constants from the
-// parameter bank).
 // Programmatic dependent launch.  The library's per-plan launches (every
 // design's kernel, the two passes of a long transform and its chunks; not the
-// persistent batch kernels) carry the programmatic-stream-serialization attribute, so
-// when the previous operation is a grid that has signalled
+// persistent batch kernels) carry the programmatic-stream-serialization
+// attribute, so when the previous operation is a grid that has signalled
 // launch_dependents, their CTAs take the SM slots its last CTAs free, with no
 // launch gap.  Every such kernel starts with grid_dep_start(): it signals its
 // own dependents (safe this early: their wait covers this whole grid and its
@@ -57,6 +55,8 @@ __device__ __forceinline__ void grid_dep_start() {
     asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
+// Per-launch arguments (by value; the kernel reads the constants from the
+// parameter bank).
 struct KArgs {
     const void* in;
     void* out;
