@@ -343,6 +343,12 @@ __host__ __device__ constexpr int window_lo(int fam, int L, int EL, int s) {
     }
     return lo;
 }
+// the first step that changes window (-1: one window)
+__host__ __device__ constexpr int first_exchange_step(int fam, int L, int EL) {
+    for (int s = 1; s < nsteps(fam, L); ++s)
+        if (window_lo(fam, L, EL, s) != window_lo(fam, L, EL, s - 1)) return s;
+    return -1;
+}
 __host__ __device__ constexpr int num_windows(int fam, int L, int EL) {
     int c = 1;
     for (int s = 1; s < nsteps(fam, L); ++s)
@@ -500,15 +506,17 @@ __device__ __forceinline__ void group_sync() {
 }
 
 // Moves the thread's registers from the window starting at bit LOA to the
-// window starting at LOB through the shared buffer sp.
+// window starting at LOB through the shared buffer sp.  lead: wait first for
+// the group's earlier reads of sp; a caller passes false (uniformly) when no
+// thread has touched sp since the last barrier of the whole CTA.
 template <int L, int EL, int LOA, int LOB>
-__device__ __forceinline__ void exchange_windows(int (&v)[1 << EL], int* sp, int g) {
+__device__ __forceinline__ void exchange_windows(int (&v)[1 << EL], int* sp, int g, bool lead = true) {
     constexpr int E = 1 << EL, G = 1 << (L - EL);
     constexpr int OLO = LOA > LOB ? LOA : LOB;
     constexpr int OHI = (LOA < LOB ? LOA : LOB) + EL;
     constexpr int W = OHI > OLO ? OHI - OLO : 0;
     constexpr int VB = W >= 2 ? 2 : W;
-    group_sync<G>();
+    if (lead) group_sync<G>();
     if constexpr (VB == 0) {
         constexpr XPad X = scalar_layout(L, EL, LOA, LOB);
         int* const pa = sp + xpad(posmap<LOA, EL>(g, 0), X.s, X.t);
@@ -581,8 +589,11 @@ __device__ __forceinline__ void exchange_cols(int (&v)[1 << EL], int* sp, int g,
 // XC > 0: column pass (XC columns per CTA, exchanges through exchange_cols);
 // HIB: row pass, the polynomial is row `hi` of a longer transform and the
 // twiddle block index carries hi in its top bits.
+// fresh: no thread of the CTA has touched sp since the CTA's last barrier, so
+// the transform's first exchange needs no leading barrier (uniform)
 template <int FAM, int L, int EL, int S, int XC = 0, bool HIB = false>
-__device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const KC& a, int hi = 0, int cl = 0) {
+__device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const KC& a, int hi = 0, int cl = 0,
+                                        bool fresh = false) {
     constexpr int E = 1 << EL;
     constexpr int G = 1 << (L - EL);
     constexpr int LO = window_lo(FAM, L, EL, S);
@@ -594,7 +605,7 @@ __device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const
         constexpr int PLO = window_lo(FAM, L, EL, S - 1);
         if constexpr (PLO != LO) {
             if constexpr (XC > 0) exchange_cols<L, EL, PLO, LO, XC>(v, sp, g, cl);
-            else exchange_windows<L, EL, PLO, LO>(v, sp, g);
+            else exchange_windows<L, EL, PLO, LO>(v, sp, g, !(fresh && S == first_exchange_step(FAM, L, EL)));
         }
     }
     const int q = a.q;
@@ -797,9 +808,9 @@ __device__ __forceinline__ void do_step(int (&v)[1 << EL], int* sp, int g, const
 }
 
 template <int FAM, int L, int EL, int... S>
-__device__ __forceinline__ void run_steps(int (&v)[1 << EL], int* sp, int g, const KC& a,
+__device__ __forceinline__ void run_steps(int (&v)[1 << EL], int* sp, int g, const KC& a, bool fresh,
                                           std::integer_sequence<int, S...>) {
-    (do_step<FAM, L, EL, S>(v, sp, g, a), ...);
+    (do_step<FAM, L, EL, S>(v, sp, g, a, 0, 0, fresh), ...);
 }
 
 template <int FAM, int L, int EL, int XC, bool HIB, int... S>
@@ -958,14 +969,21 @@ __device__ __forceinline__ void k_ntt_body(const KArgs& a) {
     }
     // bit-reversed input: the radix-4 inverse reads bit-reversed order unless
     // the input is natural; the other inverse designs read natural order on request
+    bool fresh = true;   // the exchange buffer is untouched until the transform's first exchange
     if constexpr (BR) {
-        if (!a.natural_in) permute_br<L, EL, LO0>(v, sp, g);
+        if (!a.natural_in) {
+            permute_br<L, EL, LO0>(v, sp, g);
+            fresh = false;
+        }
     } else if constexpr (fam_natural_in(FAM, BR)) {
-        if (a.natural_in) permute_br<L, EL, LO0>(v, sp, g);
+        if (a.natural_in) {
+            permute_br<L, EL, LO0>(v, sp, g);
+            fresh = false;
+        }
     }
     prologue<FAM>(v, a);
     const KC kc = make_kc(a);
-    run_steps<FAM, L, EL>(v, sp, g, kc, std::make_integer_sequence<int, NS>{});
+    run_steps<FAM, L, EL>(v, sp, g, kc, fresh, std::make_integer_sequence<int, NS>{});
     epilogue<FAM, BR>(v, a);
     if constexpr (BR) {
         permute_br<L, EL, LOZ>(v, sp, g);

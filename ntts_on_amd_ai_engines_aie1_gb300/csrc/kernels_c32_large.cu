@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(P << (L2 - EL)) k_crows(const __grid_constant_
         prologue<FAM>(v, a);                                   // raw input (the first pass)
     }
     const KC kc = make_kc(a);
-    run_steps<FAM, L2, EL>(v, sp, g, kc, std::make_integer_sequence<int, NS>{});
+    run_steps<FAM, L2, EL>(v, sp, g, kc, true, std::make_integer_sequence<int, NS>{});   // sp untouched so far
     if (!active) return;                                       // no exchange follows
     if constexpr (FWD) {
         epilogue<FAM, false>(v, a);                            // the forward's last pass

@@ -198,16 +198,24 @@ __device__ __forceinline__ void tile_transform(void* stage, int* xbuf, const KC&
         for (int k = 0; k < E; ++k) v[k] = 0;
     }
     prologue<FAM>(v, ka);
+    // The exchange buffer was last read before the barrier that ends the
+    // caller's previous tile (or never), so the tile's first exchange needs no
+    // leading barrier.
+    bool fresh = true;
     if constexpr (LO0 != LOS) {
         // the CTA agrees on the path (natural_in is the segment's): every
         // thread takes the exchange or none does
         if constexpr (RUN_READ) {
-            if (!__syncthreads_or(in_window)) exchange_windows<L, EL, LOS, LO0>(v, sp, g);
+            if (!__syncthreads_or(in_window)) {
+                exchange_windows<L, EL, LOS, LO0>(v, sp, g, false);
+                fresh = false;
+            }
         } else {
-            exchange_windows<L, EL, LOS, LO0>(v, sp, g);
+            exchange_windows<L, EL, LOS, LO0>(v, sp, g, false);
+            fresh = false;
         }
     }
-    run_steps<FAM, L, EL>(v, sp, g, a, std::make_integer_sequence<int, NS>{});
+    run_steps<FAM, L, EL>(v, sp, g, a, fresh, std::make_integer_sequence<int, NS>{});
     epilogue<FAM, false>(v, ka);
     if (!active) return;
     if constexpr (fam_natural_out(FAM, false)) {
