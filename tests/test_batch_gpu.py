@@ -351,3 +351,37 @@ def test_batch_graph_with_two_pass_segments(gb):
         b.status()
         for i, ((_, _, y), w) in enumerate(zip(segs, wants)):
             assert torch.equal(y, w), (i, rep)
+
+
+@pytest.mark.parametrize("force", ["5,0", "4,0", "4,4"])
+def test_canonical_int32_batch_every_configuration(gb, orc, monkeypatch, force):
+    """Every compiled canonical int32 configuration, pinned with
+    GBNTT_TUNE_FORCE (32 or 16 coefficients per thread; registers for 2 or 4
+    CTAs/SM).  Forward and inverse, natural order, n^-1 scaling, n = 4 .. 4096,
+    full-range inputs: outputs against the exact transform."""
+    monkeypatch.setenv("GBNTT_TUNE_FORCE", force)
+    rng = np.random.default_rng(SEED + 90)
+    specs = [(4, 4096, 998244353, 37, 0), (5, 2048, 754974721, 21, 0x10), (4, 256, 469762049, 301, 0x8),
+             (5, 1024, 167772161, 45, 0x8), (5, 4, 998244353, 777, 0)]
+    segs, wants = [], []
+    for kind, n, q, count, fl in specs:
+        root = root_for(q, n)
+        x = rng.integers(-(1 << 31), 1 << 31, (count, n)).astype(np.int32)
+        d = torch.from_numpy(x).cuda()
+        segs.append((gb.Plan(kind, n, q, root, 0, gb.FLAG_CANONICAL | fl), d, torch.full_like(d, 3)))
+        inverse = kind == 5
+        xin = np.ascontiguousarray(x[:, orc.bitrev_perm(n)]) if (fl & 0x8 and inverse) else x
+        w = orc.ntt_exact(xin, q, root, inverse=inverse)
+        if fl & 0x10:
+            w = w * pow(n, -1, q) % q
+        if fl & 0x8 and not inverse:
+            w = w[:, orc.bitrev_perm(n)]
+        wants.append(w)
+    b = gb.Batch(segs)
+    assert b.launches == 1
+    for rep in range(2):
+        b.graph_launch()
+        torch.cuda.synchronize()
+        b.status()
+        for i, ((_, _, y), w) in enumerate(zip(segs, wants)):
+            assert np.array_equal(y.cpu().numpy().astype(np.int64), w.astype(np.int64)), (force, i, rep)
