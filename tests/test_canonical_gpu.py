@@ -221,6 +221,38 @@ def test_canonical_int32_four_step(gb, orc, q, L):
     assert np.array_equal(yi, y)
 
 
+# the largest NTT primes below 2^30 (the canonical int32 family's bound: lanes
+# below 2q, sums below 4q < 2^32) for a given 2-adic order: (q, generator, n)
+Q30_EDGE = [(1073692673, 3, 4096), (1073692673, 3, 16384), (1073479681, 11, 1 << 16),
+            (1073479681, 11, 1 << 18), (1053818881, 7, 1 << 20)]
+
+
+@pytest.mark.parametrize("q,g,n", Q30_EDGE)
+def test_canonical_int32_moduli_just_below_2_30(gb, orc, q, g, n):
+    """Full-range int32 inputs at the largest moduli the canonical int32
+    family takes, where its lazy bounds are tightest: per-plan (n = 4096, one
+    CTA per polynomial at 2^14) and four-step (2^16 .. 2^20) forward, the
+    inverse with the fused n^-1, and the persistent batch at n = 4096."""
+    root = pow(g, (q - 1) // n, q)
+    rng = np.random.default_rng(SEED + 4200 + n.bit_length())
+    batch = 1 if n >= 1 << 18 else 3
+    x = inputs(rng, batch, n, -(1 << 31), 1 << 31, np.int32)
+    y = gpu_run(gb, 4, n, q, root, x, flags=gb.FLAG_CANONICAL)
+    assert np.array_equal(y.astype(np.int64), orc.ntt_exact(x, q, root))
+    w = gpu_run(gb, 5, n, q, root, y, flags=gb.FLAG_CANONICAL | gb.FLAG_SCALE_NINV)
+    assert np.array_equal(w.astype(np.int64), x.astype(np.int64) % q)
+    if n == 4096:
+        xs = rng.integers(-(1 << 31), 1 << 31, (40, n)).astype(np.int32)
+        d = torch.from_numpy(xs).cuda()
+        out = torch.empty_like(d)
+        b = gb.Batch([(gb.Plan(4, n, q, root, 0, gb.FLAG_CANONICAL), d, out)])
+        assert b.launches == 1
+        b.execute()
+        torch.cuda.synchronize()
+        b.status()
+        assert np.array_equal(out.cpu().numpy().astype(np.int64), orc.ntt_exact(xs, q, root))
+
+
 def test_canonical_four_step_status_and_many_chunks(gb, orc):
     """A batch spanning three L2 chunks (96 MiB, 24 polynomials of 2^20, each;
     programmatic dependent launches between the passes and the chunks) and the

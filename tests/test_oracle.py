@@ -217,7 +217,8 @@ def test_full_barrett(orc):
 
 
 @pytest.mark.parametrize("q,g,n", [(12289, 11, 256), (7681, 17, 512), (998244353, 3, 128),
-                                   (1073707009, 0, 64), (469762049, 3, 2)])
+                                   (1073707009, 0, 64), (469762049, 3, 2),
+                                   (1073692673, 3, 256), (1073479681, 11, 128), (1053818881, 7, 64)])
 def test_exact_transform_is_the_dft(orc, q, g, n):
     """oracle.ntt_exact (the canonical families' checker) against the O(n^2)
     definition: forward in bit-reversed order, inverse from bit-reversed input,
