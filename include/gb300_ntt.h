@@ -25,6 +25,15 @@
  * d_out (in place) is allowed.  Plans are immutable after creation and may be
  * used from several host threads and streams at once.  Every function returns
  * a gbntt_status; gbntt_last_error() gives a message for the calling thread.
+ *
+ * Launch ordering.  The per-plan launches (gbntt_execute's kernels) are
+ * programmatic dependent launches: each kernel first signals that the next
+ * grid on the stream may start, then waits for the previous grid's completion
+ * and memory before it touches global memory, so calls that follow one another
+ * on a stream start without a launch gap.  A caller's own kernel that follows
+ * and is launched with cudaLaunchAttributeProgrammaticStreamSerialization must
+ * call cudaGridDependencySynchronize() before it reads this library's outputs,
+ * as the attribute requires; every other operation is ordered as usual.
  */
 #ifndef GB300_NTT_H
 #define GB300_NTT_H
