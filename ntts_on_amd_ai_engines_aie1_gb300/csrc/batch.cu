@@ -143,8 +143,10 @@ int autotune(gbntt_batch* b) {
         if (p.layouts.size() < 2) continue;
         for (size_t c = 0; c < p.layouts.size() && rc == GBNTT_OK; ++c)
             for (int w = 0; w < 2 && rc == GBNTT_OK; ++w) rc = launch_layout(b, i, p.layouts[c], s);
-        // three interleaved rounds, best round per configuration (clock drift hits all alike)
-        for (int round = 0; round < 3 && rc == GBNTT_OK; ++round) {
+        // five interleaved rounds, best round per configuration (clock drift
+        // hits all alike; configurations 3 % apart were ranked inconsistently
+        // with three)
+        for (int round = 0; round < 5 && rc == GBNTT_OK; ++round) {
             for (size_t c = 0; c < p.layouts.size() && rc == GBNTT_OK; ++c) {
                 float ms = 0.f;
                 if (flush) {
