@@ -74,6 +74,27 @@ def test_mixed_batch(gb):
             assert np.array_equal(got, want), f"segment {i} ({SEGS[i][:5]}), repetition {rep}"
 
 
+def test_mixed_batch_graph_replay(gb):
+    """The mixed batch (persistent launches, then the bit-reversal and radix-8
+    stage plan launches, which are programmatic dependent launches) captured
+    in the batch's CUDA graph and replayed."""
+    rng = np.random.default_rng(SEED + 5)
+    made = [_make(gb, rng, s) for s in SEGS]
+    xs = [torch.from_numpy(x).cuda() for _, x, _ in made]
+    ys = [torch.full_like(x, 12345) for x in xs]
+    b = gb.Batch([(p, x, y) for (p, _, _), x, y in zip(made, xs, ys)])
+    s = torch.cuda.Stream()
+    for rep in range(3):
+        with torch.cuda.stream(s):
+            for y in ys:
+                y.fill_(12345)
+        b.graph_launch(s)
+        s.synchronize()
+        b.status()
+        for i, ((_, _, want), y) in enumerate(zip(made, ys)):
+            assert np.array_equal(y.cpu().numpy(), want), f"segment {i} ({SEGS[i][:5]}), replay {rep}"
+
+
 def test_graph_launch_and_rebind(gb):
     rng = np.random.default_rng(SEED + 1)
     made = [_make(gb, rng, s) for s in SEGS[:4]]
