@@ -147,28 +147,44 @@ int autotune(gbntt_batch* b) {
         // hits all alike; configurations 3 % apart were ranked inconsistently
         // with three)
         for (int round = 0; round < 5 && rc == GBNTT_OK; ++round) {
-            for (size_t c = 0; c < p.layouts.size() && rc == GBNTT_OK; ++c) {
-                float ms = 0.f;
-                if (flush) {
-                    // three launches, each after the flush, each timed alone
+            if (flush) {
+                // every configuration three times, each launch after the fill
+                // and timed alone, the whole round enqueued before one wait:
+                // the launches meet the GPU as timed steps do (the next one
+                // queued while the fill runs), not after an idle gap
+                const size_t nl = p.layouts.size() * 3;
+                std::vector<cudaEvent_t> ev(2 * nl);
+                for (auto& x : ev) cudaEventCreate(&x);
+                for (size_t c = 0; c < p.layouts.size() && rc == GBNTT_OK; ++c)
                     for (int w = 0; w < 3 && rc == GBNTT_OK; ++w) {
                         cudaMemsetAsync(flush, w, flush_bytes, s);
-                        cudaEventRecord(e0, s);
+                        cudaEventRecord(ev[2 * (3 * c + w)], s);
                         rc = launch_layout(b, i, p.layouts[c], s);
-                        cudaEventRecord(e1, s);
-                        if (cudaEventSynchronize(e1) != cudaSuccess) rc = batch_fail(GBNTT_ERR_CUDA, "autotune timing");
+                        cudaEventRecord(ev[2 * (3 * c + w) + 1], s);
+                    }
+                if (rc == GBNTT_OK && cudaStreamSynchronize(s) != cudaSuccess)
+                    rc = batch_fail(GBNTT_ERR_CUDA, "autotune timing");
+                for (size_t c = 0; c < p.layouts.size() && rc == GBNTT_OK; ++c) {
+                    float ms = 0.f;
+                    for (int w = 0; w < 3; ++w) {
                         float one = 0.f;
-                        cudaEventElapsedTime(&one, e0, e1);
+                        cudaEventElapsedTime(&one, ev[2 * (3 * c + w)], ev[2 * (3 * c + w) + 1]);
                         ms += one / 3.f;
                     }
-                } else {
-                    cudaEventRecord(e0, s);
-                    for (int w = 0; w < 5 && rc == GBNTT_OK; ++w) rc = launch_layout(b, i, p.layouts[c], s);
-                    cudaEventRecord(e1, s);
-                    if (cudaEventSynchronize(e1) != cudaSuccess) rc = batch_fail(GBNTT_ERR_CUDA, "autotune timing");
-                    cudaEventElapsedTime(&ms, e0, e1);
-                    ms /= 5.f;
+                    if (p.layouts[c].ms < 0.f || ms < p.layouts[c].ms) p.layouts[c].ms = ms;
                 }
+                for (auto& x : ev) cudaEventDestroy(x);
+                continue;
+            }
+            // inputs larger than L2: five launches back to back
+            for (size_t c = 0; c < p.layouts.size() && rc == GBNTT_OK; ++c) {
+                float ms = 0.f;
+                cudaEventRecord(e0, s);
+                for (int w = 0; w < 5 && rc == GBNTT_OK; ++w) rc = launch_layout(b, i, p.layouts[c], s);
+                cudaEventRecord(e1, s);
+                if (cudaEventSynchronize(e1) != cudaSuccess) rc = batch_fail(GBNTT_ERR_CUDA, "autotune timing");
+                cudaEventElapsedTime(&ms, e0, e1);
+                ms /= 5.f;
                 if (p.layouts[c].ms < 0.f || ms < p.layouts[c].ms) p.layouts[c].ms = ms;
             }
         }
