@@ -716,6 +716,10 @@ PROFILE_CASES = {
     "c_r2f32_1m": (4, 1 << 20, 998244353, 565042129, 64, 1),
     "c_r2g32_1m": (5, 1 << 20, 998244353, 565042129, 64, 1),
     "c_r2f32_64k": (4, 1 << 16, 998244353, pow(3, (998244353 - 1) >> 16, 998244353), 1024, 1),
+    # the stand-alone units (HBM-bound): bit reversal, full Barrett multiplication by n^-1
+    "bitrev_4096": (6, 4096, 12289, 0, 65536),
+    "fullbarrett_4096": (7, 4096, 12289, 0, 65536),
+    "r8stage_4096": (3, 4096, 12289, 41, 65536),
     "batch_r4": None,   # the benchmark batch, 4x larger, persistent kernel
     "c_batch_r4": None,  # the same with GBNTT_FLAG_CANONICAL
 }
@@ -760,7 +764,8 @@ def run_profile_case(name, launches=3):
     if name == "c_batch_r4":
         return run_profile_batch(4, launches, flags=1)
     kind, n, q, root, polys, *fl = PROFILE_CASES[name]
-    plan = gb.Plan(kind, n, q, root, 0, fl[0] if fl else 0)
+    factor = pow(n, -1, q) if kind == 7 else 0        # the full Barrett unit multiplies by n^-1
+    plan = gb.Plan(kind, n, q, root, factor, fl[0] if fl else 0)
     dt = torch.int32 if plan.elem_bytes == 4 else torch.int16
     g = torch.Generator(device="cuda").manual_seed(SEED)
     x = torch.randint(0, q, (polys, n), dtype=torch.int64, device="cuda", generator=g).to(dt)

@@ -131,8 +131,10 @@ def test_r2_i32(gb, orc, n, q):
     check(gb, orc, gb.Kind.R2_I32_INV, orc.R2_I32_INV, n, q, root, xf)
 
 
-@pytest.mark.parametrize("n", [2, 8, 256, 512, 1024, 2048, 4096, 8192, 65536])
+@pytest.mark.parametrize("n", [2, 8, 64, 128, 256, 512, 1024, 2048, 4096, 8192, 65536])
 def test_bitrev(gb, orc, n):
+    """Out of place and in place; n = 64 .. 4096 run the tiled transpose
+    kernel, the others the staged gather."""
     rng = np.random.default_rng(SEED + 700 + n)
     x = inputs(rng, 5, n, -32768, 32768, np.int16)
     got = gpu_run(gb, gb.Kind.BITREV_I16, n, 0, 0, x)
@@ -140,6 +142,17 @@ def test_bitrev(gb, orc, n):
     assert np.array_equal(got, want)
     got2 = gpu_run(gb, gb.Kind.BITREV_I16, n, 0, 0, x, inplace=True)
     assert np.array_equal(got2, want)
+
+
+@pytest.mark.parametrize("n", [64, 128, 256, 2048, 4096])
+def test_bitrev_many_polynomials(gb, orc, n):
+    """The tiled kernel with several tiles per CTA and a partly filled last
+    CTA (301 polynomials), out of place and in place."""
+    rng = np.random.default_rng(SEED + 750 + n)
+    x = inputs(rng, 301, n, -32768, 32768, np.int16)
+    want = orc.Plan(orc.BITREV_I16, n)(x)
+    assert np.array_equal(gpu_run(gb, gb.Kind.BITREV_I16, n, 0, 0, x), want)
+    assert np.array_equal(gpu_run(gb, gb.Kind.BITREV_I16, n, 0, 0, x, inplace=True), want)
 
 
 @pytest.mark.parametrize("n,batch", [(4096, 3), (1024, 17), (7, 5)])
