@@ -13,59 +13,89 @@ namespace {
 // polynomial p reads x[i + M m] (M = n/8), forms y_k = sum_m x_m F8[m][k] in
 // int32, reduces y_k with twiddle root^(i k) and writes the eight results
 // (de-interleaved and 3-bit reversed, :152-154) as one 16-byte store at 8 i.
+// W = 2: a thread takes two adjacent i (n >= 16), so its inputs arrive as
+// 4-byte pairs, its twiddles as 16-byte pairs and its outputs leave as two
+// 16-byte stores (65536 x 4096: 2.9 TB/s with one i per thread).
+template <int W>
 __global__ void __launch_bounds__(256) k_r8_stage(const KArgs a, int L) {
     grid_dep_start();
     const int n = 1 << L, M = n >> 3;
-    const long long total = a.batch << (L - 3);
+    const int GL = L - 3 - (W == 2 ? 1 : 0);             // log2 thread groups per polynomial
+    const long long total = a.batch << GL;
     const short* in = static_cast<const short*>(a.in);
     short* out = static_cast<short*>(a.out);
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
-        const long long poly = idx >> (L - 3);
-        const int i = (int)(idx & (M - 1));
+        const long long poly = idx >> GL;
+        const int i = (int)(idx & ((1 << GL) - 1)) * W;
         const short* src = in + poly * n + i;
-        int x[8], y[8];
+        int x[W][8], y[W][8];
 #pragma unroll
-        for (int m = 0; m < 8; ++m) x[m] = __ldg(src + m * M);
-        if (a.r8_sym) {
-            const int f1 = a.f8s[1], f2 = a.f8s[2], f3 = a.f8s[3];
-            const int a0 = x[0] + x[4], a1 = x[1] + x[5], a2 = x[2] + x[6], a3 = x[3] + x[7];
-            const int b0 = x[0] - x[4], b1 = x[1] - x[5], b2 = x[2] - x[6], b3 = x[3] - x[7];
-            const int c0 = a0 + a2, c1 = a1 + a3, d0 = a0 - a2, d1 = a1 - a3;
-            y[0] = c0 + c1;
-            y[4] = c0 - c1;
-            const int t2 = f2 * d1;
-            y[2] = d0 + t2;
-            y[6] = d0 - t2;
-            const int e0 = b0 + f2 * b2, e1 = b0 - f2 * b2;
-            const int h1 = f1 * b1 + f3 * b3, h3 = f3 * b1 + f1 * b3;
-            y[1] = e0 + h1;
-            y[5] = e0 - h1;
-            y[3] = e1 + h3;
-            y[7] = e1 - h3;
-        } else {
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                int acc = 0;
-#pragma unroll
-                for (int m = 0; m < 8; ++m) acc += x[m] * a.f8[8 * m + k];
-                y[k] = acc;
+        for (int m = 0; m < 8; ++m) {
+            if constexpr (W == 2) {
+                const int v = __ldg(reinterpret_cast<const int*>(src + m * M));
+                x[0][m] = (short)(v & 0xFFFF);
+                x[1][m] = v >> 16;
+            } else {
+                x[0][m] = __ldg(src + m * M);
             }
         }
-        int o[8];
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            if (a.r8_sym) {
+                const int f1 = a.f8s[1], f2 = a.f8s[2], f3 = a.f8s[3];
+                const int* xw = x[w];
+                const int a0 = xw[0] + xw[4], a1 = xw[1] + xw[5], a2 = xw[2] + xw[6], a3 = xw[3] + xw[7];
+                const int b0 = xw[0] - xw[4], b1 = xw[1] - xw[5], b2 = xw[2] - xw[6], b3 = xw[3] - xw[7];
+                const int c0 = a0 + a2, c1 = a1 + a3, d0 = a0 - a2, d1 = a1 - a3;
+                y[w][0] = c0 + c1;
+                y[w][4] = c0 - c1;
+                const int t2 = f2 * d1;
+                y[w][2] = d0 + t2;
+                y[w][6] = d0 - t2;
+                const int e0 = b0 + f2 * b2, e1 = b0 - f2 * b2;
+                const int h1 = f1 * b1 + f3 * b3, h3 = f3 * b1 + f1 * b3;
+                y[w][1] = e0 + h1;
+                y[w][5] = e0 - h1;
+                y[w][3] = e1 + h3;
+                y[w][7] = e1 - h3;
+            } else {
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    int acc = 0;
+#pragma unroll
+                    for (int m = 0; m < 8; ++m) acc += x[w][m] * a.f8[8 * m + k];
+                    y[w][k] = acc;
+                }
+            }
+        }
+        int o[W][8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            const int2 t = __ldg(&a.tab[k * M + i]);
-            int z = r8red(y[k], t.x, t.y, a.q);
-            if (a.canonical) z = canon(z, a.q, a.canon_c);
-            o[brev_c<3>(k)] = z;
+            int2 t[W];
+            if constexpr (W == 2) {
+                const int4 tt = __ldg(reinterpret_cast<const int4*>(&a.tab[k * M + i]));
+                t[0] = make_int2(tt.x, tt.y);
+                t[1] = make_int2(tt.z, tt.w);
+            } else {
+                t[0] = __ldg(&a.tab[k * M + i]);
+            }
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                int z = r8red(y[w][k], t[w].x, t[w].y, a.q);
+                if (a.canonical) z = canon(z, a.q, a.canon_c);
+                o[w][brev_c<3>(k)] = z;
+            }
         }
-        int4 w;
-        w.x = (o[0] & 0xFFFF) | (o[1] << 16);
-        w.y = (o[2] & 0xFFFF) | (o[3] << 16);
-        w.z = (o[4] & 0xFFFF) | (o[5] << 16);
-        w.w = (o[6] & 0xFFFF) | (o[7] << 16);
-        *reinterpret_cast<int4*>(out + poly * n + 8 * i) = w;
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            int4 v;
+            v.x = (o[w][0] & 0xFFFF) | (o[w][1] << 16);
+            v.y = (o[w][2] & 0xFFFF) | (o[w][3] << 16);
+            v.z = (o[w][4] & 0xFFFF) | (o[w][5] << 16);
+            v.w = (o[w][6] & 0xFFFF) | (o[w][7] << 16);
+            *reinterpret_cast<int4*>(out + poly * n + 8 * (i + w)) = v;
+        }
     }
 }
 
@@ -200,10 +230,12 @@ int bitrev_smem_bytes(int L) {
 }
 
 cudaError_t launch_r8_stage(const KArgs& a, int L, cudaStream_t s) {
-    const long long work = a.batch << (L - 3);
+    const bool pair = L >= 4;
+    const long long work = a.batch << (L - 3 - (pair ? 1 : 0));
     KArgs ka = a;
     void* args[] = {&ka, &L};
-    return launch_kernel(reinterpret_cast<const void*>(&k_r8_stage), grid_for(work, 256), 256, 0, args, s, true);
+    const void* fn = pair ? reinterpret_cast<const void*>(&k_r8_stage<2>) : reinterpret_cast<const void*>(&k_r8_stage<1>);
+    return launch_kernel(fn, grid_for(work, 256), 256, 0, args, s, true);
 }
 
 cudaError_t launch_bitrev(const KArgs& a, int L, cudaStream_t s) {

@@ -92,7 +92,7 @@ def test_r4_inverse(gb, orc, n):
     check(gb, orc, gb.Kind.R4_I16_INV, orc.R4_I16_INV, n, q, root_for(q, n), x)
 
 
-@pytest.mark.parametrize("n", [16, 64, 512, 1024, 4096])
+@pytest.mark.parametrize("n", [16, 32, 64, 512, 1024, 4096])
 def test_r8_stage_reference_multipliers(gb, orc, n):
     """The reference's one radix-8 stage with its float K=31 multipliers:
     bit-exact, including the outputs those multipliers get wrong."""
