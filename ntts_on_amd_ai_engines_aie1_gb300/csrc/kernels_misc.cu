@@ -126,8 +126,8 @@ __global__ void __launch_bounds__(256) k_bitrev(const KArgs a, int L, int P) {
     }
 }
 
-// Bit reversal of 2^L coefficients (6 <= L <= 12) as a transpose.  With
-// K = floor(L/2), m = L - 2K middle bits and the index split as (a, b, c) --
+// Bit reversal of 2^L coefficients (L >= 6) as a transpose.  With
+// K = min(floor(L/2), 6), m = L - 2K middle bits and the index split as (a, b, c) --
 // a the top K bits, b the m middle ones, c the bottom K -- the reversed index
 // is (bitrev(c), bitrev(b), bitrev(a)): for each b, the 2^K x 2^K tile
 // in[a][c] lands transposed, both indices reversed, at out[bitrev(c)][bitrev(a)].
@@ -239,8 +239,10 @@ cudaError_t launch_r8_stage(const KArgs& a, int L, cudaStream_t s) {
 }
 
 cudaError_t launch_bitrev(const KArgs& a, int L, cudaStream_t s) {
-    if (L >= 6 && L <= 12) {   // buffers are 16-byte aligned (checked by the caller)
-        const int K = L / 2;
+    // buffers are 16-byte aligned (checked by the caller); beyond 2^12 a
+    // polynomial's tiles spread over several CTAs, so only out of place
+    if (L >= 6 && (L <= 12 || a.in != a.out)) {
+        const int K = L / 2 < 6 ? L / 2 : 6;
         const long long ntiles = a.batch << (L - 2 * K);
         const int tpc = 2 * K >= 12 ? 1 : 4096 >> (2 * K);
         const unsigned grid = (unsigned)((ntiles + tpc - 1) / tpc);
