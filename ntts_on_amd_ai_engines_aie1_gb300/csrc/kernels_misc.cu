@@ -102,7 +102,9 @@ __global__ void __launch_bounds__(256) k_r8_stage(const KArgs a, int L) {
 // Bit-reversal unit (src/kernels/bitreverse_kernels.cc:54-143):
 // out[bitrev(i)] = in[i].  P polynomials per CTA are staged in shared memory
 // with coalesced 16-byte loads, then written back in order, each thread
-// reading the bit-reversed source position from shared memory.
+// reading the bit-reversed source position from shared memory.  Used for
+// n < 64 and for n >= 2^13 in place (a whole polynomial per CTA); the tiled
+// k_bitrev_t below, free of its bank conflicts, takes every other case.
 __global__ void __launch_bounds__(256) k_bitrev(const KArgs a, int L, int P) {
     grid_dep_start();
     extern __shared__ short sb[];
