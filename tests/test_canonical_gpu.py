@@ -305,3 +305,51 @@ for name, kind, fl in (("canon_fwd", 4, gb.FLAG_CANONICAL), ("canon_inv", 5, gb.
     assert r.returncode == 0, r.stdout + r.stderr
     for name, w in want.items():
         assert np.array_equal(np.load(tmp_path / (name + ".npy")), w), name
+
+
+def test_four_step_for_2_14_and_2_15_when_asked(gb, orc, tmp_path):
+    """GBNTT_FOURSTEP_MIN_L=14 (read once per process) moves n = 2^14 and 2^15
+    to the four-step (column pass of 4 and 8 rows): a child process checks
+    forward, inverse with n^-1 and in-place runs against the exact transform."""
+    import os
+    import subprocess
+    import sys
+    q = 998244353
+    rng = np.random.default_rng(SEED + 4300)
+    cases = []
+    for L in (14, 15):
+        n = 1 << L
+        x = rng.integers(-(1 << 31), 1 << 31, (3, n)).astype(np.int32)
+        np.save(tmp_path / f"x{L}.npy", x)
+        cases.append((L, x))
+    root_dir = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    child = f"""
+import numpy as np, torch, sys
+sys.path.insert(0, {root_dir!r})
+import ntts_on_amd_ai_engines_aie1_gb300 as gb
+q = {q}
+for L in (14, 15):
+    n = 1 << L
+    root = pow(3, (q - 1) >> L, q)
+    x = torch.from_numpy(np.load({str(tmp_path)!r} + f"/x{{L}}.npy")).cuda()
+    f = gb.Plan(4, n, q, root, 0, gb.FLAG_CANONICAL)
+    i = gb.Plan(5, n, q, root, 0, gb.FLAG_CANONICAL | gb.FLAG_SCALE_NINV)
+    y = f(x)
+    z = i(y)
+    w = x.clone()
+    f.execute(w, w, w.shape[0])
+    torch.cuda.synchronize()
+    f.status(); i.status()
+    np.save({str(tmp_path)!r} + f"/y{{L}}.npy", y.cpu().numpy())
+    np.save({str(tmp_path)!r} + f"/z{{L}}.npy", z.cpu().numpy())
+    np.save({str(tmp_path)!r} + f"/w{{L}}.npy", w.cpu().numpy())
+"""
+    env = dict(os.environ, GBNTT_FOURSTEP_MIN_L="14")
+    r = subprocess.run([sys.executable, "-c", child], env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    for L, x in cases:
+        root = pow(3, (q - 1) >> L, q)
+        want = orc.ntt_exact(x, q, root)
+        assert np.array_equal(np.load(tmp_path / f"y{L}.npy").astype(np.int64), want), L
+        assert np.array_equal(np.load(tmp_path / f"w{L}.npy").astype(np.int64), want), L
+        assert np.array_equal(np.load(tmp_path / f"z{L}.npy").astype(np.int64), x.astype(np.int64) % q), L
